@@ -1,0 +1,204 @@
+/*
+ * sop_gpu.h -- C ABI of libsopgpu.so, the GB300 (sm_103a) SOP engine.
+ *
+ * The reference (samchogroup/SOP) has no plugin API: its device side is a set
+ * of free functions over process globals (energy.h:13-24, sop.h:23-60,
+ * GPUvars.h:148-152).  This header is the boundary that replaces that device
+ * side.  Plain pointers and sizes only; every call returns an int status
+ * (SOP_OK = 0).  Host pointers are borrowed for the duration of a call.
+ *
+ * One context is one CUDA stream on one device.  A context holds one or more
+ * independent molecules (trajectories); the reference's plain path is a
+ * context with one molecule, the batched ensemble a context with many.  Calls
+ * on one context are not thread-safe; separate contexts may run on separate
+ * host threads.
+ *
+ * Indices are 0-based.  The reference stores 1-based 14-bit bead indices with
+ * a 2-bit type (global.h:51-67); the engine keeps untyped 32-bit indices and a
+ * per-bead type array, so molecules may exceed the reference's 16,383 beads.
+ */
+#ifndef SOP_GPU_H
+#define SOP_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes (the reference calls exit(-1) instead: energy.cu:149,165,
+ * sop.cu:1002-1006, 1257-1261). */
+enum {
+  SOP_OK = 0,
+  SOP_ERR_ARG = 1,        /* invalid argument or call order */
+  SOP_ERR_CUDA = 2,       /* a CUDA runtime call failed */
+  SOP_ERR_ALLOC = 3,      /* device allocation failed */
+  SOP_ERR_CAPACITY = 4,   /* a list outgrew its capacity and could not be regrown */
+  SOP_ERR_MOLECULE = 5,   /* a molecule stopped: FENE bond beyond R0 or a non-finite value */
+  SOP_ERR_BUDGET = 6,     /* admission refused: the HBM budget is exhausted */
+  SOP_ERR_NOT_FOUND = 7   /* unknown molecule id */
+};
+
+/* Per-molecule status bits (sop_molecule_status). */
+enum {
+  SOP_MOL_FENE_RANGE = 1, /* |r - r0| >= R0 on some bond: log(1 - dev^2/R0^2) undefined */
+  SOP_MOL_NONFINITE = 2,  /* a force or coordinate became NaN/Inf */
+  SOP_MOL_DONE = 4        /* reached its step budget */
+};
+
+/*
+ * Force field, integrator and list parameters (the reference's globals set by
+ * alloc_arrays and set_params, param.cpp:8-119, 233-394).
+ *
+ * List cut-offs: a positive *_fac selects the reference's factor mode, where
+ * the cut-off is fac * r0 for native pairs and fac * sigma_rep for non-native
+ * pairs (sop.cu:746-749, 815-818, 861-864, 910-913: 3.2 for the neighbour
+ * list, 2.5 for the pair list); *_fac <= 0 selects an absolute cut-off of
+ * *_abs Angstrom.  Membership is d^2 < rcut^2, with d^2 formed in FP32 as the
+ * reference's host filters do.
+ *
+ * Cadence: the neighbour list is rebuilt before step n when n % nnlup == 0
+ * (sop.cu:200-225), the pair list when n % nplup == 0 or after a neighbour-list
+ * rebuild (the reference rebuilds it every step, nplup = 1, sop.cu:227-232).
+ */
+typedef struct sop_params {
+  double k_bnd;       /* FENE k, kcal/mol/A^2 (param.cpp:14) */
+  double R0;          /* FENE R0, A (param.cpp:15) */
+  double eps_ss;      /* i,i+2 soft-sphere epsilon (param.cpp:37) */
+  double sigma_ss;    /* i,i+2 soft-sphere sigma, A (param.cpp:35) */
+  double eps_rep;     /* non-native repulsion epsilon (energy.cu:15-19) */
+  double boxl;        /* periodic box length, A (param.cpp:97) */
+  double h;           /* time step, tau_L (param.cpp:104, set t_step) */
+  double zeta;        /* friction, 1/tau_L (param.cpp:100) */
+  double nl_att_fac, nl_att_abs, nl_rep_fac, nl_rep_abs;
+  double pl_att_fac, pl_att_abs, pl_rep_fac, pl_rep_abs;
+  int nnlup;          /* neighbour-list cadence, steps (param.cpp:103) */
+  int nplup;          /* pair-list cadence, steps */
+  int rep6;           /* 0: eps (s^12/r^12 + s^6/r^6) as energy.cu:436-437; 1: eps (s/r)^6 */
+  int device;         /* CUDA device ordinal (set device, param.cpp:387-390) */
+  int graph_steps;    /* steps per captured CUDA graph (0: the engine's default) */
+  int lanes_per_bead; /* 0: autotuned table; else 1,2,4,8,16 or 32 */
+  unsigned long long seed; /* Philox key (replaces setup_rng's seed, GPUvars.cu:417-453) */
+} sop_params;
+
+/* Fills *p with the reference's defaults and the factor-mode list cut-offs. */
+void sop_params_default(sop_params* p);
+
+/*
+ * One molecule: what the reference's bonds/angles/vdw/init files hold
+ * (io.cpp:112-259).  Non-native pairs are implicit: every pair with
+ * |i - j| > 2 that is not a native contact (the content of the reference's
+ * idx_bead_lj_non_nat, io.cpp:216-225).
+ */
+typedef struct sop_molecule {
+  int nbead;
+  int nbnd;  const int* bond_i; const int* bond_j; const float* bond_r0;
+  int nang;  const int* ang_i;  const int* ang_k;          /* soft sphere on (i, k) */
+  int nnat;  const int* nat_i;  const int* nat_j; const float* nat_r0;
+  const float* nat_eps;        /* epsilon of the native force; NULL: 1.0 */
+  const float* nat_eps_energy; /* epsilon of the native energy; NULL: nat_eps */
+  const int* types;            /* per bead 1 or 2 (sigma_rep table); NULL: all 1 */
+  const float* unc_pos;        /* 3*nbead unwrapped coordinates (required) */
+  const float* pos;            /* 3*nbead wrapped coordinates; NULL: unc_pos */
+  const float* vel;            /* 3*nbead; NULL: zero (sop.cu:117-128) */
+  double T;                    /* kBT, kcal/mol (param.cpp:92, set temp) */
+  unsigned int traj;           /* Philox stream id of this trajectory */
+  long long nsteps;            /* step budget; < 0: unlimited */
+} sop_molecule;
+
+/* Context lifetime: replaces alloc_GPU_arrays / alloc_cudpp / setup_rng
+ * (GPUvars.cu:99-293, 417-453). */
+int sop_ctx_create(const sop_params* p, void** ctx);
+int sop_ctx_destroy(void* ctx);
+
+/* Stages a molecule; *mol_id receives its id.  Device state is created by
+ * sop_commit. */
+int sop_add_molecule(void* ctx, const sop_molecule* m, int* mol_id);
+
+/*
+ * Uploads every staged molecule, builds the neighbour and pair lists from the
+ * initial coordinates and evaluates the initial forces: the set-up half of
+ * underdamped_ctrl (sop.cu:133-186: alloc_GPU_arrays, setup_rng,
+ * update_neighbor_list, update_pair_list, force_eval).
+ */
+int sop_commit(void* ctx);
+
+/* Single-molecule convenience: sop_add_molecule + sop_commit. */
+int sop_upload_topology(void* ctx, const sop_molecule* m);
+
+/* Replaces coordinates and velocities of molecule `mol` (load_coords /
+ * load_vels H2D, io.cpp:361-363, 407) and re-evaluates its forces. */
+int sop_upload_state(void* ctx, int mol, const float* pos, const float* unc_pos,
+                     const float* vel);
+
+/*
+ * Advances every active molecule nsteps Langevin steps: the loop body of
+ * underdamped_ctrl (sop.cu:197-243) -- list rebuilds on their cadence,
+ * underdamped_iteration_kernel, force_eval, update_velocities_kernel
+ * (sop.cu:421-484) -- run as fused kernels in captured CUDA graphs.
+ */
+int sop_step(void* ctx, long long nsteps);
+
+/* Rebuilds the neighbour lists now (update_neighbor_list, sop.cu:928-1262);
+ * returns the attractive / repulsive totals over all molecules (pairs, each
+ * counted once) when the pointers are non-NULL. */
+int sop_update_neighbor_list(void* ctx, long long* nnl_att, long long* nnl_rep);
+
+/* Rebuilds the pair lists from the neighbour lists (update_pair_list,
+ * sop.cu:1456-1706). */
+int sop_update_pair_list(void* ctx, long long* nil_att, long long* nil_rep);
+
+/* Re-evaluates forces at the current coordinates, noise included
+ * (force_eval + random_force, energy.cu:81-167). */
+int sop_force_eval(void* ctx);
+
+/*
+ * Noise injection: with normals != NULL the next force evaluation uses
+ * force += sqrt(2 T zeta / h) * normals[3*i + c] for every bead i of every
+ * molecule (beads numbered across molecules in id order) instead of the
+ * Philox stream; NULL returns to Philox.  Replaces random_force's
+ * generator (energy.cu:154-188) for single-step parity checks.
+ */
+int sop_set_noise(void* ctx, const float* normals);
+
+/* Copies molecule `mol`'s current state to host arrays of 3*nbead floats;
+ * NULL pointers are skipped (the D2H reads of sop.cu:252-263). */
+int sop_download(void* ctx, int mol, float* pos, float* unc_pos, float* vel, float* force);
+
+/*
+ * Copies molecule `mol`'s lists as (i, j) pairs with i < j, 0-based.
+ * which: 0 attractive neighbour list, 1 repulsive neighbour list,
+ *        2 attractive pair list,      3 repulsive pair list.
+ * cap is the capacity of i_out / j_out (and r0_out for the attractive lists,
+ * NULL allowed); *count receives the list size even when it exceeds cap.
+ */
+int sop_download_list(void* ctx, int mol, int which, long long cap, int* i_out, int* j_out,
+                      float* r0_out, long long* count);
+
+/*
+ * Energy terms of molecule `mol` on its current pair lists (energy_eval and
+ * the host energies of energy.cu:69-78, 194-225, 278-307, 369-442), per-term
+ * FP32 evaluation with an FP64 final sum.  terms: e_bnd, e_ang_ss,
+ * e_vdw_rr_att, e_vdw_rr_rep, rna_etot.
+ */
+int sop_energy(void* ctx, int mol, double* terms);
+
+/* Observables of calculate_observables (sop.cu:528-611): Q, rgsq, kinT,
+ * contct_nat, with FP64 reductions. */
+int sop_observables(void* ctx, int mol, double* out);
+
+/* Molecule status bits (SOP_MOL_*) and its completed step count. */
+int sop_molecule_status(void* ctx, int mol, int* status, long long* step);
+
+/* Total device bytes held by the context, and the bytes charged to `mol`. */
+int sop_memory(void* ctx, int mol, long long* ctx_bytes, long long* mol_bytes);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that time or order
+ * work around the engine. */
+int sop_stream(void* ctx, void** stream);
+
+/* Last error message of the context (or of the library when ctx is NULL). */
+const char* sop_last_error(void* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SOP_GPU_H */

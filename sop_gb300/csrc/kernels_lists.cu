@@ -1,0 +1,532 @@
+// Neighbour-list and pair-list rebuilds (replace update_neighbor_list /
+// update_pair_list, sop.cu:704-920, 928-1262, 1456-1706, and the CUDPP radix
+// sort + scan they use).
+//
+// Neighbour list (every nnlup steps):
+//   1. per-molecule bounding box of the coordinates             k_bbox
+//   2. per-molecule cell grid (cell edge rc/S, S=1..4 chosen so a cell holds
+//      ~1.5 beads; molecules whose extent + rc reaches boxl, where the minimum
+//      image matters, fall back to index-chunked cells that scan all pairs)
+//                                                                k_grid, k_grid_base
+//   3. counting sort of beads into cells (own scan), cells sorted by bead id
+//      so every later order is deterministic                     k_assign, scan, k_scatter, k_cellsort
+//   4. 8 lanes per bead in cell order: the bead against the beads of the
+//      cell rows within S along each axis, culled to its own cut-off sphere;
+//      predicate = the reference's FP32 host filter (d^2 < rcut^2, |i-j| > 2,
+//      not native); one pass writes fixed-stride rows (overflow: regrow) k_nl
+//   The attractive neighbour list filters each bead's native row (k_assign).
+// Pair list (every nplup steps): warp per bead compacts its neighbour-list row
+// in place order (k_pl).
+#include "sop_dev.cuh"
+
+namespace sop {
+
+// ------------------------------------------------------------------ scan
+// Exclusive scan of n ints: out[0..n], out[n] = total.  Three kernels:
+// per-block reduce, one-block scan of the block sums, per-block apply.
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int warp_incl_scan(int v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the exclusive
+// prefix and the block total in *total.
+__device__ __forceinline__ int block_excl_scan(int v, int* total) {
+  __shared__ int warp_sums[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int incl = warp_incl_scan(v);
+  if (lane == 31) warp_sums[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    int s = lane < nw ? warp_sums[lane] : 0;
+    int si = warp_incl_scan(s);
+    if (lane < nw) warp_sums[lane] = si - s;
+    if (lane == 31) warp_sums[31] = si;  // total (nw <= 32)
+  }
+  __syncthreads();
+  int res = incl - v + warp_sums[w];
+  *total = warp_sums[31];
+  __syncthreads();
+  return res;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const int* __restrict__ in, long long n,
+                                                               int* __restrict__ block_sums) {
+  long long base = (long long)blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k)
+    if (base + k < n) s += in[base + k];
+  int total;
+  block_excl_scan(s, &total);
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_top(int* __restrict__ block_sums, int nblocks) {
+  int carry = 0;
+  for (int b0 = 0; b0 < nblocks; b0 += blockDim.x) {
+    int b = b0 + threadIdx.x;
+    int v = b < nblocks ? block_sums[b] : 0;
+    int total;
+    int ex = block_excl_scan(v, &total);
+    if (b < nblocks) block_sums[b] = ex + carry;
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int* __restrict__ in, long long n,
+                                                              const int* __restrict__ block_sums,
+                                                              int* __restrict__ out) {
+  long long base = (long long)blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  int v[kScanItems];
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    v[k] = (base + k < n) ? in[base + k] : 0;
+    s += v[k];
+  }
+  int total;
+  int ex = block_excl_scan(s, &total) + block_sums[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    if (base + k < n) out[base + k] = ex;
+    ex += v[k];
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[n] = ex;
+}
+
+// ---------------------------------------------------------------- grids
+__global__ void k_bbox_reset(DevSys s) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= s.nmol) return;
+  unsigned* b = s.bbox + 6 * m;
+  b[0] = b[1] = b[2] = f2ord(INFINITY);
+  b[3] = b[4] = b[5] = f2ord(-INFINITY);
+}
+
+__device__ __forceinline__ bool mol_listed(const DevSys& s, int m) {
+  return m >= 0 && s.mol[m].active && s.mol_status[m] == 0;
+}
+
+// Coordinates at step mol_step + koff (the positions the rebuild uses).
+__device__ __forceinline__ const float4* xbuf(const DevSys& s, int m, int koff) {
+  return s.x[(int)((s.mol_step[m] + koff) & 1)];
+}
+
+__global__ void k_bbox(DevSys s, int koff) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int m = (i < s.nbead) ? s.mol_of[i] : -1;
+  bool ok = mol_listed(s, m);
+  unsigned act = __ballot_sync(0xffffffffu, ok);
+  if (!ok) return;
+  float4 x = xbuf(s, m, koff)[i];
+  unsigned peers = __match_any_sync(act, m);
+  unsigned lo[3] = {f2ord(x.x), f2ord(x.y), f2ord(x.z)};
+  unsigned mn[3], mx[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    mn[a] = __reduce_min_sync(peers, lo[a]);
+    mx[a] = __reduce_max_sync(peers, lo[a]);
+  }
+  if ((threadIdx.x & 31) == __ffs(peers) - 1) {
+    unsigned* b = s.bbox + 6 * m;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      atomicMin(b + a, mn[a]);
+      atomicMax(b + 3 + a, mx[a]);
+    }
+  }
+}
+
+// One thread per molecule: cell grid of its neighbour-list build.
+__global__ void k_grid(DevSys s, int* __restrict__ ncell) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= s.nmol) return;
+  MolGrid g = {};
+  int n = s.mol[m].n;
+  if (!mol_listed(s, m) || n <= 0) {
+    g.ncell = 0;
+    s.grid[m] = g;
+    ncell[m] = 0;
+    return;
+  }
+  const unsigned* b = s.bbox + 6 * m;
+  float lo[3], ext[3];
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = ord2f(b[a]);
+    ext[a] = ord2f(b[3 + a]) - lo[a];
+  }
+  const float rc = s.rc_nl_rep_max;
+  bool periodic = false;
+  for (int a = 0; a < 3; ++a) periodic |= !(ext[a] + rc < s.boxl);  // also true for NaN extents
+  if (periodic || n <= 96) {
+    // every pair is scanned; cells are chunks of 32 consecutive beads
+    g.brute = 1;
+    g.dims[0] = (n + 31) / 32; g.dims[1] = 1; g.dims[2] = 1;
+    g.S = g.dims[0];
+    g.cs = 0.0f;
+    g.lo[0] = g.lo[1] = g.lo[2] = 0.0f;
+  } else {
+    float vol = fmaxf((ext[0] + 1.0f) * (ext[1] + 1.0f) * (ext[2] + 1.0f), 1.0f);
+    float rho = (float)n / vol;
+    int S = (int)floorf(rc * cbrtf(rho * (1.0f / 1.5f)));
+    S = S < 1 ? 1 : (S > 4 ? 4 : S);
+    float cs = rc * 1.0001f / (float)S + 1.0e-4f;
+    long long cap = n * 2 > 64 ? (long long)n * 2 : 64;
+    for (int iter = 0; iter < 8; ++iter) {
+      long long tot = 1;
+      for (int a = 0; a < 3; ++a) {
+        g.dims[a] = (int)floorf(ext[a] / cs) + 1;
+        tot *= g.dims[a];
+      }
+      if (tot <= cap) break;
+      cs *= cbrtf((float)tot / (float)cap) * 1.01f;
+      S = (int)ceilf(rc * 1.0001f / cs);
+      if (S < 1) S = 1;
+    }
+    g.brute = 0;
+    g.S = S;
+    g.cs = cs;
+    for (int a = 0; a < 3; ++a) g.lo[a] = lo[a];
+  }
+  g.ncell = g.dims[0] * g.dims[1] * g.dims[2];
+  s.grid[m] = g;
+  ncell[m] = g.ncell;
+}
+
+// Single block: cell bases = exclusive scan of the per-molecule cell counts;
+// flags overflow of the cell capacity (cannot happen by construction: each
+// molecule holds at most max(64, 2n) cells, and the capacity is their sum).
+__global__ void __launch_bounds__(1024) k_grid_base(DevSys s, const int* __restrict__ ncell,
+                                                     int* __restrict__ cells_total) {
+  int carry = 0;
+  for (int b0 = 0; b0 < s.nmol; b0 += blockDim.x) {
+    int m = b0 + threadIdx.x;
+    int v = m < s.nmol ? ncell[m] : 0;
+    int total;
+    int ex = block_excl_scan(v, &total);
+    if (m < s.nmol) s.grid[m].base = ex + carry;
+    carry += total;
+  }
+  if (threadIdx.x == 0) {
+    if (carry > s.cell_cap) atomicOr(s.flags, FLAG_NL_OVERFLOW);
+    *cells_total = carry > s.cell_cap ? (int)s.cell_cap : carry;
+  }
+}
+
+__device__ __forceinline__ int cell_coord(float v, float lo, float cs, int dim) {
+  int c = (int)floorf((v - lo) / cs);
+  return c < 0 ? 0 : (c >= dim ? dim - 1 : c);
+}
+
+// Per bead: cell index and slot (counting sort), plus the attractive
+// neighbour-list filter of its native row (sop.cu:704-759 semantics).
+__global__ void k_assign(DevSys s, int koff) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.nbead) return;
+  int m = s.mol_of[i];
+  if (!mol_listed(s, m)) {
+    s.bead_cell[i] = -1;
+    s.nl_att_cnt[i] = 0;
+    return;
+  }
+  const float4* X = xbuf(s, m, koff);
+  float4 xi = X[i];
+  MolGrid g = s.grid[m];
+  int c;
+  if (g.brute) {
+    c = g.base + (i - s.mol[m].start) / 32;
+  } else {
+    int cx = cell_coord(xi.x, g.lo[0], g.cs, g.dims[0]);
+    int cy = cell_coord(xi.y, g.lo[1], g.cs, g.dims[1]);
+    int cz = cell_coord(xi.z, g.lo[2], g.cs, g.dims[2]);
+    c = g.base + (cz * g.dims[1] + cy) * g.dims[0] + cx;
+  }
+  if (c < 0 || c >= s.cell_cap) {  // unreachable: capacity is the sum of the per-molecule caps
+    atomicOr(s.flags, FLAG_NL_OVERFLOW);
+    s.bead_cell[i] = -1;
+    s.nl_att_cnt[i] = 0;
+    return;
+  }
+  s.bead_cell[i] = c;
+  s.bead_slot[i] = atomicAdd(s.cell_cnt + c, 1);
+  int2 row = s.nat_row[i];
+  int k = 0;
+  for (int e = 0; e < row.y; ++e) {
+    int idx = row.x + e;
+    float4 xj = X[s.nat_j[idx]];
+    float dx = min_image(__fsub_rn(xj.x, xi.x), s.boxl);
+    float dy = min_image(__fsub_rn(xj.y, xi.y), s.boxl);
+    float dz = min_image(__fsub_rn(xj.z, xi.z), s.boxl);
+    if (d2_exact(dx, dy, dz) < s.nat_rc2[idx].x) s.nl_att_e[row.x + k++] = idx;
+  }
+  s.nl_att_cnt[i] = k;
+}
+
+__global__ void k_scatter(DevSys s) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.nbead) return;
+  int c = s.bead_cell[i];
+  if (c < 0) return;
+  s.sorted[s.cell_start[c] + s.bead_slot[i]] = i;
+}
+
+// Per cell: sort its beads by id (fixes every downstream order), then stage
+// coordinates in cell order with w = (id << 2) | type.
+__global__ void k_cellsort(DevSys s, int koff, const int* __restrict__ cells_total) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= *cells_total) return;
+  int cnt = s.cell_cnt[c];
+  if (cnt == 0) return;
+  int st = s.cell_start[c];
+  int* b = s.sorted + st;
+  for (int a = 1; a < cnt; ++a) {
+    int v = b[a], k = a;
+    while (k > 0 && b[k - 1] > v) { b[k] = b[k - 1]; --k; }
+    b[k] = v;
+  }
+  for (int a = 0; a < cnt; ++a) {
+    int i = b[a];
+    int m = s.mol_of[i];
+    float4 x = xbuf(s, m, koff)[i];
+    x.w = __int_as_float((i << 2) | type_of(x));
+    s.xs[st + a] = x;
+  }
+}
+
+constexpr int kNatRegs = 16;
+constexpr int kNlLanes = 8;
+
+// Distance from v to the slab [a, a + w] (0 inside).
+__device__ __forceinline__ float slab_dist(float v, float a, float w) {
+  return fmaxf(fmaxf(a - v, v - (a + w)), 0.0f);
+}
+
+// kNlLanes lanes per bead, beads in cell order (xs), so neighbouring groups
+// share cells and candidates.  Each bead scans the cell rows (runs along x)
+// of its grid neighbourhood, culled against its own position: rows whose
+// y,z slab lies beyond the cut-off are skipped and each row's x range is
+// clipped to the chord.  Partners that pass the reference's predicate
+// (sop.cu:768-826 with the host arithmetic of sop.cu:1414-1435:
+// d^2 < (fac*sigma or abs)^2 in FP32, |i - j| > 2, not a native contact) are
+// written to the bead's fixed-stride row in candidate order (group ballot).
+// The culling is conservative (a 1e-3 A margin); membership is decided by the
+// exact predicate alone.  The bead's native partners sit in registers.
+__global__ void __launch_bounds__(256) k_nl(DevSys s) {
+  const int k = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) / kNlLanes);
+  const int lane = threadIdx.x % kNlLanes;
+  const unsigned wl = threadIdx.x & 31;
+  const unsigned gmask = ((1u << kNlLanes) - 1u) << (wl & ~(kNlLanes - 1u));
+  const unsigned below = (1u << wl) - 1u;
+  if (k >= s.cell_start[s.cell_cap]) return;   // beads that were binned
+  if (*s.flags & FLAG_NL_OVERFLOW) return;
+  const float4 xi = s.xs[k];
+  const int wi = __float_as_int(xi.w);
+  const int i = wi >> 2, ti = wi & 3;
+  const int m = s.mol_of[i];
+  const MolGrid g = s.grid[m];
+  const int lc = s.bead_cell[i] - g.base;
+  const int nx = g.dims[0], ny = g.dims[1], nz = g.dims[2];
+  const int cx = lc % nx, cy = (lc / nx) % ny, cz = lc / (nx * ny);
+  const int z0 = max(cz - g.S, 0), z1 = min(cz + g.S, nz - 1);
+  const int y0 = max(cy - g.S, 0), y1 = min(cy + g.S, ny - 1);
+  const int x0 = max(cx - g.S, 0), x1 = min(cx + g.S, nx - 1);
+  const float boxl = s.boxl;
+  const float r11 = s.rc2_nl_rep[1][1], r12 = s.rc2_nl_rep[1][2], r22 = s.rc2_nl_rep[2][2];
+  const float rcm = s.rc_nl_rep_max * 1.0001f + 1.0e-3f;
+  const float rcm2 = rcm * rcm;
+  const int2 nrow = s.nat_row[i];
+  int nat[kNatRegs];
+#pragma unroll
+  for (int q = 0; q < kNatRegs; ++q) nat[q] = q < nrow.y ? s.nat_j[nrow.x + q] : -1;
+  const long long stride = s.nl_stride;
+  int* row = s.nl_j + (long long)i * stride;
+  int cnt = 0;
+  for (int z = z0; z <= z1; ++z) {
+    const float dz = g.brute ? 0.0f : slab_dist(xi.z, g.lo[2] + z * g.cs, g.cs);
+    if (dz * dz > rcm2) continue;
+    for (int y = y0; y <= y1; ++y) {
+      const float dy = g.brute ? 0.0f : slab_dist(xi.y, g.lo[1] + y * g.cs, g.cs);
+      const float rem = rcm2 - dz * dz - dy * dy;
+      if (rem < 0.0f) continue;
+      int xa = x0, xb = x1;
+      if (!g.brute) {
+        const float w = sqrtf(rem);
+        xa = max(x0, cell_coord(xi.x - w, g.lo[0], g.cs, nx));
+        xb = min(x1, cell_coord(xi.x + w, g.lo[0], g.cs, nx));
+      }
+      const int rowc = g.base + (z * ny + y) * nx;
+      const int ja = s.cell_start[rowc + xa];
+      const int jb = s.cell_start[rowc + xb] + s.cell_cnt[rowc + xb];
+      for (int jc = ja; jc < jb; jc += kNlLanes) {
+        const int jj = jc + lane;
+        bool pass = false;
+        int j = 0;
+        if (jj < jb) {
+          const float4 xj = s.xs[jj];
+          const int wj = __float_as_int(xj.w);
+          j = wj >> 2;
+          if (abs(j - i) > 2) {
+            const float dx = min_image(__fsub_rn(xj.x, xi.x), boxl);
+            const float dy2 = min_image(__fsub_rn(xj.y, xi.y), boxl);
+            const float dz2 = min_image(__fsub_rn(xj.z, xi.z), boxl);
+            pass = d2_exact(dx, dy2, dz2) < pick_type_pair(r11, r12, r22, ti, wj & 3);
+            if (pass) {
+              bool native = false;
+#pragma unroll
+              for (int q = 0; q < kNatRegs; ++q) native |= (nat[q] == j);
+              for (int q = kNatRegs; q < nrow.y && !native; ++q) native = (s.nat_j[nrow.x + q] == j);
+              pass = !native;
+            }
+          }
+        }
+        const unsigned msk = __ballot_sync(gmask, pass);
+        if (pass) {
+          const int pos = cnt + __popc(msk & below);
+          if (pos < stride) row[pos] = j;
+        }
+        cnt += __popc(msk);
+      }
+    }
+  }
+  if (lane == 0) {
+    s.nl_cnt[i] = cnt < stride ? cnt : (int)stride;
+    if (cnt > stride) {
+      atomicOr(s.flags, FLAG_NL_OVERFLOW);
+      atomicMax(s.nl_maxrow, cnt);
+    }
+  }
+}
+
+// Warp per bead: the pair list is the in-order compaction of the bead's
+// neighbour-list row by the pair-list cut-off (sop.cu:835-920 semantics,
+// host arithmetic of sop.cu:1737-1810).  Each lane takes 4 consecutive
+// entries per iteration (one 16-byte load, four independent gathers) and a
+// warp scan places the survivors; the attractive pair list is the same over
+// the bead's attractive neighbour list.
+__global__ void __launch_bounds__(256) k_pl(DevSys s, int koff) {
+  const int lane = threadIdx.x & 31;
+  const int i = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (i >= s.nbead) return;
+  if (*s.flags & FLAG_NL_OVERFLOW) return;
+  const int m = s.mol_of[i];
+  if (!mol_listed(s, m)) {
+    if (lane == 0) { s.pl_cnt[i] = 0; s.pl_att_cnt[i] = 0; }
+    return;
+  }
+  const float4* X = xbuf(s, m, koff);
+  const float4 xi = X[i];
+  const int ti = type_of(xi);
+  const float boxl = s.boxl;
+  const float r11 = s.rc2_pl_rep[1][1], r12 = s.rc2_pl_rep[1][2], r22 = s.rc2_pl_rep[2][2];
+  const unsigned lt = (1u << lane) - 1u;
+  const long long a = (long long)i * s.nl_stride;
+  const int4* row4 = reinterpret_cast<const int4*>(s.nl_j + a);
+  int* out = s.pl_j + a;
+  const int cnt = s.nl_cnt[i];
+  const int2 row = s.nat_row[i];
+  const int acnt = s.nl_att_cnt[i];
+  int k = 0;
+  for (int e0 = 0; e0 < cnt; e0 += 128) {
+    const int e = e0 + 4 * lane;
+    int4 jv = make_int4(i, i, i, i);
+    if (e < cnt) jv = row4[(e0 >> 2) + lane];
+    const int jq[4] = {jv.x, e + 1 < cnt ? jv.y : i, e + 2 < cnt ? jv.z : i, e + 3 < cnt ? jv.w : i};
+    bool pq[4];
+    int c = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 xj = X[e + q < cnt ? jq[q] : i];
+      const float dx = min_image(__fsub_rn(xj.x, xi.x), boxl);
+      const float dy = min_image(__fsub_rn(xj.y, xi.y), boxl);
+      const float dz = min_image(__fsub_rn(xj.z, xi.z), boxl);
+      pq[q] = (e + q < cnt) && d2_exact(dx, dy, dz) < pick_type_pair(r11, r12, r22, ti, type_of(xj));
+      c += pq[q] ? 1 : 0;
+    }
+    int incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    int pos = k + incl - c;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (pq[q]) out[pos++] = jq[q];
+    k += __shfl_sync(0xffffffffu, incl, 31);
+  }
+  if (lane == 0) s.pl_cnt[i] = k;
+  int ka = 0;
+  for (int e0 = 0; e0 < acnt; e0 += 32) {
+    const int e = e0 + lane;
+    bool pass = false;
+    int idx = 0, j = 0;
+    if (e < acnt) {
+      idx = s.nl_att_e[row.x + e];
+      j = s.nat_j[idx];
+      float4 xj = X[j];
+      float dx = min_image(__fsub_rn(xj.x, xi.x), boxl);
+      float dy = min_image(__fsub_rn(xj.y, xi.y), boxl);
+      float dz = min_image(__fsub_rn(xj.z, xi.z), boxl);
+      pass = d2_exact(dx, dy, dz) < s.nat_rc2[idx].y;
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, pass);
+    if (pass) {
+      float4 q = s.nat_par[idx];
+      s.pl_att[row.x + ka + __popc(mask & lt)] = make_float4(__int_as_float(j), q.x, q.y, q.z);
+    }
+    ka += __popc(mask);
+  }
+  if (lane == 0) s.pl_att_cnt[i] = ka;
+}
+
+// ------------------------------------------------------------ host side
+static inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
+
+// Launch sequence of an exclusive scan of n ints (in -> out[0..n]).
+void launch_scan(const int* in, long long n, int* out, int* block_sums, cudaStream_t st) {
+  unsigned nb = cdiv(n > 0 ? n : 1, kScanTile);
+  k_scan_reduce<<<nb, kScanThreads, 0, st>>>(in, n, block_sums);
+  k_scan_top<<<1, 1024, 0, st>>>(block_sums, (int)nb);
+  k_scan_apply<<<nb, kScanThreads, 0, st>>>(in, n, block_sums, out);
+}
+
+long long scan_block_sums_needed(long long n) { return cdiv(n > 0 ? n : 1, kScanTile) + 1; }
+
+struct NLScratch {
+  int* ncell;        // per molecule
+  int* block_sums;
+  int* cells_total;  // one int: cells in use
+};
+
+// Full neighbour-list rebuild from the coordinates at step mol_step + koff.
+void launch_nl_rebuild(const DevSys& s, const NLScratch& w, int koff, cudaStream_t st) {
+  const int T = 256;
+  k_bbox_reset<<<cdiv(s.nmol, T), T, 0, st>>>(s);
+  k_bbox<<<cdiv(s.nbead, T), T, 0, st>>>(s, koff);
+  k_grid<<<cdiv(s.nmol, T), T, 0, st>>>(s, w.ncell);
+  k_grid_base<<<1, 1024, 0, st>>>(s, w.ncell, w.cells_total);
+  cudaMemsetAsync(s.cell_cnt, 0, sizeof(int) * (size_t)s.cell_cap, st);
+  k_assign<<<cdiv(s.nbead, T), T, 0, st>>>(s, koff);
+  launch_scan(s.cell_cnt, s.cell_cap, s.cell_start, w.block_sums, st);
+  k_scatter<<<cdiv(s.nbead, T), T, 0, st>>>(s);
+  k_cellsort<<<cdiv(s.cell_cap, T), T, 0, st>>>(s, koff, w.cells_total);
+  k_nl<<<cdiv((long long)s.nbead * kNlLanes, T), T, 0, st>>>(s);
+}
+
+void launch_pl_rebuild(const DevSys& s, int koff, cudaStream_t st) {
+  const int T = 256;
+  k_pl<<<cdiv((long long)s.nbead * 32, T), T, 0, st>>>(s, koff);
+}
+
+}  // namespace sop

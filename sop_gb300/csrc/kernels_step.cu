@@ -1,0 +1,389 @@
+// The per-step hot path: forces (FENE, i,i+2 soft sphere, native LJ 12-6,
+// non-native repulsion), the Philox noise force and the underdamped Langevin
+// update, fused into one kernel per step.
+//
+// The reference runs per step underdamped_iteration_kernel (sop.cu:421-447),
+// clear_forces + rand_kernel + four force kernels with float atomics
+// (energy.cu:54-167, 228-584) and update_velocities_kernel (sop.cu:450-462).
+// Here a group of G lanes owns a bead: it sums the bead's force over its own
+// full rows (every pair is stored for both beads), reduces across the group
+// with shuffles, adds the noise, and updates velocity and coordinates.  No
+// atomics; the summation order is fixed by G and the row order.
+//
+// Step bookkeeping: kernel K_n computes f_n = F(x_n) + noise(n), then
+// v_n = a3 incr_n + a4 f_n, then the look-ahead incr_{n+1} = a1 v_n + a2 f_n
+// and x_{n+1} = x_n + incr_{n+1}.  This is the reference's order
+// (incr, positions, forces, velocities) regrouped so one kernel per step
+// suffices.  x_n lives in buffer n & 1, so neither the host nor a graph has
+// to track parity, and every molecule may sit at its own step.
+#include "sop_dev.cuh"
+#include "../../include/sop_gpu.h"
+
+namespace sop {
+
+template <int G>
+__device__ __forceinline__ float group_sum(float v, unsigned gmask) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(gmask, v, o);
+  return v;
+}
+
+// STEP = false: force evaluation only at step mol_step + koff (velocities kept),
+// followed by the look-ahead; used after set-up and state uploads.
+template <int G, bool STEP>
+__global__ void __launch_bounds__(256) k_step(DevSys s, const int2* __restrict__ tiles, int koff) {
+  const int2 tile = tiles[blockIdx.x];
+  const int slot = threadIdx.x / G;
+  const int lane = threadIdx.x % G;
+  if (slot >= tile.y) return;
+  if (*s.flags & FLAG_NL_OVERFLOW) return;
+  const int i = tile.x + slot;
+  const int m = s.mol_of[i];
+  if (m < 0) return;
+  const MolConst mc = s.mol[m];
+  const long long n = s.mol_step[m] + (STEP ? 1 : 0) + koff;
+  if (!mc.active || s.mol_status[m] != 0 || (STEP && mc.nsteps >= 0 && n > mc.nsteps)) return;
+  const unsigned gmask = (G == 32) ? 0xffffffffu
+                                   : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+  const int cur = (int)(n & 1);
+  const float4* __restrict__ X = s.x[cur];
+  const float4 xi = X[i];
+  const float boxl = s.boxl;
+  float fx = 0.f, fy = 0.f, fz = 0.f;
+  bool fene_bad = false;
+
+  // Row descriptors first, as independent loads.
+  const int2 br = s.bond_row[i];
+  const int2 ar = s.ang_row[i];
+  const int abase = s.nat_row[i].x;
+  const int acnt = s.pl_att_cnt[i];
+  const long long rbase = (long long)i * s.nl_stride;
+  const int rcnt = s.pl_cnt[i];
+
+  // Bonded, angle and native terms share one index space [bonds | angles |
+  // natives]; a bead has a handful of them, usually one pass of the group.
+  const int nba = br.y + ar.y;
+  const int nsmall = nba + acnt;
+  for (int e = lane; e < nsmall; e += G) {
+    int j;
+    float r0 = 0.f, eps = 0.f;
+    if (e < br.y) {
+      j = s.bond_j[br.x + e];
+      r0 = s.bond_r0[br.x + e];
+    } else if (e < nba) {
+      j = s.ang_j[ar.x + e - br.y];
+    } else {
+      const float4 q = s.pl_att[abase + e - nba];
+      j = __float_as_int(q.x);
+      r0 = q.y;
+      eps = q.z;
+    }
+    const float4 xj = X[j];
+    float lx, ly, lz;
+    const float dx = diff_exact(xj.x, xi.x, boxl, lx);
+    const float dy = diff_exact(xj.y, xi.y, boxl, ly);
+    const float dz = diff_exact(xj.z, xi.z, boxl, lz);
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    float c;
+    if (e < br.y) {
+      // FENE: force on i = +k dev / (r (1 - dev^2/R0^2)) * d  (energy.cu:252-271)
+      const float r = sqrtf(d2);
+      const float dev = d2_minus_r02(dx, dy, dz, lx, ly, lz, r0) / (r + r0);
+      const float w = 1.0f - dev * dev / s.R0sq;
+      fene_bad |= !(fabsf(dev) < s.R0);
+      c = s.k_bnd * dev / (r * w);
+    } else if (e < nba) {
+      // i,i+2 soft sphere: force on i = -6 eps sigma^6 / d^8 * d  (energy.cu:335-360)
+      const float inv = 1.0f / d2;
+      const float inv2 = inv * inv;
+      c = -s.f_ss * inv2 * inv2;
+    } else {
+      // native LJ 12-6 (energy.cu:468-507): co1 = -12 eps / d^2 (s^6 - s^3),
+      // s = r0^2 / d^2, as -12 eps / d^2 s^3 (s - 1)(s^2 + s + 1) with
+      // s - 1 = -(d^2 - r0^2) / d^2; pairs with d^2 <= 1e-7 r0^2 are skipped.
+      const float r02 = r0 * r0;
+      const float inv = 1.0f / d2;
+      const float sr = r02 * inv;
+      const float sm1 = -d2_minus_r02(dx, dy, dz, lx, ly, lz, r0) * inv;
+      const float s3 = sr * sr * sr;
+      c = (d2 > 1.0e-7f * r02) ? -12.0f * eps * inv * s3 * sm1 * (sr * sr + sr + 1.0f) : 0.0f;
+    }
+    fx += c * dx; fy += c * dy; fz += c * dz;
+  }
+
+  // Non-native repulsion (energy.cu:536-581): co1 = -6 eps / d^2 (2 (s/r)^12 +
+  // (s/r)^6) [rep6: -6 eps / d^2 (s/r)^6]; pairs with d^2 <= 1e-7 sigma are
+  // skipped.
+  const int ti = type_of(xi);
+  const float g11 = s.sig2[1][1], g12 = s.sig2[1][2], g22 = s.sig2[2][2];
+  const float ce = -6.0f * s.eps_rep;
+  const float two = s.rep6 ? 0.0f : 2.0f;
+  auto rep = [&](const float4 xj) {
+    const float dx = min_image(xj.x - xi.x, boxl);
+    const float dy = min_image(xj.y - xi.y, boxl);
+    const float dz = min_image(xj.z - xi.z, boxl);
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    const float sg2 = pick_type_pair(g11, g12, g22, ti, type_of(xj));
+    const float inv = 1.0f / d2;
+    const float u = sg2 * inv;
+    const float u3 = u * u * u;
+    const float c = (d2 > sqrtf(sg2) * 1.0e-7f) ? ce * inv * u3 * (two * u3 + 1.0f) : 0.0f;
+    fx += c * dx; fy += c * dy; fz += c * dz;
+  };
+  // Each lane takes 4 consecutive entries per iteration (one 16-byte load of
+  // the row, four independent gathers); entries past the row end read bead i
+  // itself, which the d^2 > tol test drops.
+  const int4* prow = reinterpret_cast<const int4*>(s.pl_j + rbase);
+  for (int e = 4 * lane; e < rcnt; e += 4 * G) {
+    const int4 jv = prow[e >> 2];
+    const float4 x0 = X[jv.x];
+    const float4 x1 = X[e + 1 < rcnt ? jv.y : i];
+    const float4 x2 = X[e + 2 < rcnt ? jv.z : i];
+    const float4 x3 = X[e + 3 < rcnt ? jv.w : i];
+    rep(x0);
+    rep(x1);
+    rep(x2);
+    rep(x3);
+  }
+  fx = group_sum<G>(fx, gmask);
+  fy = group_sum<G>(fy, gmask);
+  fz = group_sum<G>(fz, gmask);
+  const bool bad_any = __any_sync(gmask, fene_bad);
+  if (lane != 0) return;
+
+  float3 z;
+  if (s.use_noise) {
+    const float4 q = s.noise[i];
+    z = make_float3(q.x, q.y, q.z);
+  } else {
+    z = noise3((unsigned)(i - mc.start), n, mc.traj, s.seed_lo, s.seed_hi);
+  }
+  fx += mc.sigma_f * z.x;
+  fy += mc.sigma_f * z.y;
+  fz += mc.sigma_f * z.z;
+  int st = 0;
+  if (bad_any) st |= SOP_MOL_FENE_RANGE;
+  if (!(isfinite(fx) && isfinite(fy) && isfinite(fz))) st |= SOP_MOL_NONFINITE;
+  if (st) atomicOr(s.mol_status + m, st);
+  s.f[i] = make_float4(fx, fy, fz, 0.f);
+  float4 vi = s.v[i];
+  float4 inc = s.incr[i];
+  if (STEP && !mc.t_zero) {
+    vi = make_float4(mc.a3 * inc.x + mc.a4 * fx, mc.a3 * inc.y + mc.a4 * fy,
+                     mc.a3 * inc.z + mc.a4 * fz, 0.f);
+    s.v[i] = vi;
+  }
+  inc = make_float4(mc.a1 * vi.x + mc.a2 * fx, mc.a1 * vi.y + mc.a2 * fy,
+                    mc.a1 * vi.z + mc.a2 * fz, 0.f);
+  s.incr[i] = inc;
+  s.x[cur ^ 1][i] = make_float4(xi.x + inc.x, xi.y + inc.y, xi.z + inc.z, xi.w);
+  const float4 pi = s.p[cur][i];
+  s.p[cur ^ 1][i] = make_float4(min_image(pi.x + inc.x, boxl), min_image(pi.y + inc.y, boxl),
+                                min_image(pi.z + inc.z, boxl), 0.f);
+}
+
+// End of a block of `steps` steps: advance each running molecule's step
+// count (clamped to its budget).  A neighbour-list overflow freezes
+// everything until the host regrows the list and re-runs the block.
+__global__ void k_advance(DevSys s, int steps) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= s.nmol) return;
+  if (*s.flags & FLAG_NL_OVERFLOW) return;
+  const MolConst mc = s.mol[m];
+  if (!mc.active || s.mol_status[m] != 0) return;
+  long long st = s.mol_step[m] + steps;
+  if (mc.nsteps >= 0 && st > mc.nsteps) st = mc.nsteps;
+  s.mol_step[m] = st;
+}
+
+// ---------------------------------------------------------------- energy
+// Per-bead FP32 terms over the bead's full rows (each pair counted from both
+// beads, so halved), reduced in FP64: e_bnd, e_ang_ss, e_vdw_att, e_vdw_rep
+// (energy.cu:194-225, 278-307, 369-442).  Partial sums per block.
+__global__ void __launch_bounds__(256) k_energy(DevSys s, int mol_start, int mol_n, int m,
+                                                 double* __restrict__ part) {
+  __shared__ double red[4][8];
+  int i = mol_start + blockIdx.x * blockDim.x + threadIdx.x;
+  float eb = 0.f, ea = 0.f, eat = 0.f, erp = 0.f;
+  if (i < mol_start + mol_n) {
+    const int cur = (int)(s.mol_step[m] & 1);
+    const float4* X = s.x[cur];
+    const float4 xi = X[i];
+    const float boxl = s.boxl;
+    const int2 br = s.bond_row[i];
+    for (int e = 0; e < br.y; ++e) {
+      const float4 xj = X[s.bond_j[br.x + e]];
+      const float r0 = s.bond_r0[br.x + e];
+      float lx, ly, lz;
+      float dx = diff_exact(xj.x, xi.x, boxl, lx), dy = diff_exact(xj.y, xi.y, boxl, ly),
+            dz = diff_exact(xj.z, xi.z, boxl, lz);
+      float r = sqrtf(dx * dx + dy * dy + dz * dz);
+      float dev = d2_minus_r02(dx, dy, dz, lx, ly, lz, r0) / (r + r0);
+      eb += log1pf(-dev * dev / s.R0sq);
+    }
+    const int2 ar = s.ang_row[i];
+    for (int e = 0; e < ar.y; ++e) {
+      const float4 xj = X[s.ang_j[ar.x + e]];
+      float dx = min_image(xj.x - xi.x, boxl), dy = min_image(xj.y - xi.y, boxl),
+            dz = min_image(xj.z - xi.z, boxl);
+      float inv = 1.0f / (dx * dx + dy * dy + dz * dz);
+      ea += s.e_ss * inv * inv * inv;
+    }
+    const int abase = s.nat_row[i].x, acnt = s.pl_att_cnt[i];
+    for (int e = 0; e < acnt; ++e) {
+      const float4 q = s.pl_att[abase + e];
+      const float4 xj = X[__float_as_int(q.x)];
+      float lx, ly, lz;
+      float dx = diff_exact(xj.x, xi.x, boxl, lx), dy = diff_exact(xj.y, xi.y, boxl, ly),
+            dz = diff_exact(xj.z, xi.z, boxl, lz);
+      float d2 = dx * dx + dy * dy + dz * dz;
+      float sr = q.y * q.y / d2;
+      float s3 = sr * sr * sr;
+      float sm1 = -d2_minus_r02(dx, dy, dz, lx, ly, lz, q.y) / d2;
+      // eps_e (s^6 - 2 s^3) = eps_e (s^3 (s^3 - 1) - s^3)
+      eat += q.w * (s3 * sm1 * (sr * sr + sr + 1.0f) - s3);
+    }
+    const long long rbase = (long long)i * s.nl_stride;
+    const int rcnt = s.pl_cnt[i];
+    const int ti = type_of(xi);
+    for (int e = 0; e < rcnt; ++e) {
+      const float4 xj = X[s.pl_j[rbase + e]];
+      float dx = min_image(xj.x - xi.x, boxl), dy = min_image(xj.y - xi.y, boxl),
+            dz = min_image(xj.z - xi.z, boxl);
+      float u = s.sig2[ti][type_of(xj)] / (dx * dx + dy * dy + dz * dz);
+      float u3 = u * u * u;
+      erp += s.rep6 ? s.eps_rep * u3 : s.eps_rep * u3 * (u3 + 1.0f);
+    }
+  }
+  double v[4] = {0.5 * (double)eb, 0.5 * (double)ea, 0.5 * (double)eat, 0.5 * (double)erp};
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    double x = v[t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) red[t][w] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double x = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) x += red[threadIdx.x][k];
+    part[4 * blockIdx.x + threadIdx.x] = x;
+  }
+}
+
+// Final FP64 sum of the per-block partials, in block order.
+__global__ void k_energy_final(const double* __restrict__ part, int nblocks, double k_bnd_R0sq_half,
+                               double* __restrict__ out) {
+  if (threadIdx.x >= 4) return;
+  double x = 0.0;
+  for (int b = 0; b < nblocks; ++b) x += part[4 * b + threadIdx.x];
+  if (threadIdx.x == 0) x *= -k_bnd_R0sq_half;  // e_bnd = -(k R0^2 / 2) sum log(...)
+  out[threadIdx.x] = x;
+}
+
+// ----------------------------------------------------------- observables
+// Q over all native contacts (each counted from its lower bead), the
+// first and second moments of the coordinates for Rg^2, and sum v^2, in FP64
+// (sop.cu:528-611).  Partials per block: {contacts, sx, sy, sz, sxx, svv}.
+__global__ void __launch_bounds__(256) k_observables(DevSys s, int mol_start, int mol_n, int m,
+                                                      double* __restrict__ part) {
+  __shared__ double red[6][8];
+  int i = mol_start + blockIdx.x * blockDim.x + threadIdx.x;
+  double v[6] = {0, 0, 0, 0, 0, 0};
+  if (i < mol_start + mol_n) {
+    const int cur = (int)(s.mol_step[m] & 1);
+    const float4* X = s.x[cur];
+    const float4 xi = X[i];
+    const int2 nr = s.nat_row[i];
+    int cnt = 0;
+    for (int e = 0; e < nr.y; ++e) {
+      int j = s.nat_j[nr.x + e];
+      if (j < i) continue;
+      const float4 xj = X[j];
+      float dx = min_image(__fsub_rn(xi.x, xj.x), s.boxl);
+      float dy = min_image(__fsub_rn(xi.y, xj.y), s.boxl);
+      float dz = min_image(__fsub_rn(xi.z, xj.z), s.boxl);
+      float d = sqrtf(d2_exact(dx, dy, dz));
+      if (__fdiv_rn(d, s.nat_par[nr.x + e].x) < 1.25f) ++cnt;
+    }
+    const float4 vi = s.v[i];
+    v[0] = cnt;
+    v[1] = xi.x; v[2] = xi.y; v[3] = xi.z;
+    v[4] = (double)xi.x * xi.x + (double)xi.y * xi.y + (double)xi.z * xi.z;
+    v[5] = (double)vi.x * vi.x + (double)vi.y * vi.y + (double)vi.z * vi.z;
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    double x = v[t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) red[t][w] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double x = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) x += red[threadIdx.x][k];
+    part[6 * blockIdx.x + threadIdx.x] = x;
+  }
+}
+
+__global__ void k_observables_final(const double* __restrict__ part, int nblocks, int n, int nnat,
+                                    double* __restrict__ out) {
+  if (threadIdx.x != 0) return;
+  double t[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = 0; b < nblocks; ++b)
+    for (int k = 0; k < 6; ++k) t[k] += part[6 * b + k];
+  const double inv = 1.0 / n;
+  const double mx = t[1] * inv, my = t[2] * inv, mz = t[3] * inv;
+  out[0] = nnat ? t[0] / nnat : 0.0;                           // Q
+  out[1] = t[4] * inv - (mx * mx + my * my + mz * mz);         // rgsq = sum_{i<j} d^2 / N^2
+  out[2] = t[5] / (3.0 * n);                                   // kinT
+  out[3] = t[0];                                               // contct_nat
+}
+
+// ----------------------------------------------------------- launchers
+static inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
+
+template <int G>
+static void launch_step_g(const DevSys& s, const int2* tiles, int ntiles, int koff, bool step,
+                          cudaStream_t st) {
+  if (ntiles <= 0) return;
+  if (step)
+    k_step<G, true><<<ntiles, 256, 0, st>>>(s, tiles, koff);
+  else
+    k_step<G, false><<<ntiles, 256, 0, st>>>(s, tiles, koff);
+}
+
+void launch_step(const DevSys& s, int G, const int2* tiles, int ntiles, int koff, bool step,
+                 cudaStream_t st) {
+  switch (G) {
+    case 1: launch_step_g<1>(s, tiles, ntiles, koff, step, st); break;
+    case 2: launch_step_g<2>(s, tiles, ntiles, koff, step, st); break;
+    case 4: launch_step_g<4>(s, tiles, ntiles, koff, step, st); break;
+    case 8: launch_step_g<8>(s, tiles, ntiles, koff, step, st); break;
+    case 16: launch_step_g<16>(s, tiles, ntiles, koff, step, st); break;
+    default: launch_step_g<32>(s, tiles, ntiles, koff, step, st); break;
+  }
+}
+
+void launch_advance(const DevSys& s, int steps, cudaStream_t st) {
+  k_advance<<<cdiv(s.nmol, 256), 256, 0, st>>>(s, steps);
+}
+
+void launch_energy(const DevSys& s, int mol_start, int mol_n, int m, double* part, double* out,
+                   double k_bnd_R0sq_half, cudaStream_t st) {
+  int nb = (int)cdiv(mol_n, 256);
+  k_energy<<<nb, 256, 0, st>>>(s, mol_start, mol_n, m, part);
+  k_energy_final<<<1, 32, 0, st>>>(part, nb, k_bnd_R0sq_half, out);
+}
+
+void launch_observables(const DevSys& s, int mol_start, int mol_n, int m, int nnat, double* part,
+                        double* out, cudaStream_t st) {
+  int nb = (int)cdiv(mol_n, 256);
+  k_observables<<<nb, 256, 0, st>>>(s, mol_start, mol_n, m, part);
+  k_observables_final<<<1, 32, 0, st>>>(part, nb, mol_n, nnat, out);
+}
+
+}  // namespace sop

@@ -1,0 +1,274 @@
+"""Python binding of libsopgpu.so (include/sop_gpu.h) through ctypes.
+
+This is a thin host-side mirror of the engine's C ABI; every computation runs
+in the CUDA library.  Importing works without a GPU; creating a context
+requires the built library and a CUDA device and raises otherwise -- there is
+no CPU fallback.
+
+Reference correspondence (samchogroup/SOP):
+  Engine(...) + add()/commit()  alloc_GPU_arrays, setup_rng, initial lists and
+                                force_eval of underdamped_ctrl (sop.cu:133-186)
+  step(n)                       the loop body of underdamped_ctrl (sop.cu:197-243)
+  update_neighbor_list()        update_neighbor_list (sop.cu:928-1262)
+  update_pair_list()            update_pair_list (sop.cu:1456-1706)
+  force_eval()                  force_eval (energy.cu:81-150)
+  energy()                      energy_eval (energy.cu:69-78)
+  observables()                 calculate_observables (sop.cu:528-611)
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .system import Molecule
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+SOP_OK = 0
+STATUS_NAMES = {1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_ALLOC", 4: "ERR_CAPACITY",
+                5: "ERR_MOLECULE", 6: "ERR_BUDGET", 7: "ERR_NOT_FOUND"}
+MOL_FENE_RANGE, MOL_NONFINITE, MOL_DONE = 1, 2, 4
+
+
+class SopError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("k_bnd", ctypes.c_double), ("R0", ctypes.c_double),
+                ("eps_ss", ctypes.c_double), ("sigma_ss", ctypes.c_double),
+                ("eps_rep", ctypes.c_double), ("boxl", ctypes.c_double),
+                ("h", ctypes.c_double), ("zeta", ctypes.c_double),
+                ("nl_att_fac", ctypes.c_double), ("nl_att_abs", ctypes.c_double),
+                ("nl_rep_fac", ctypes.c_double), ("nl_rep_abs", ctypes.c_double),
+                ("pl_att_fac", ctypes.c_double), ("pl_att_abs", ctypes.c_double),
+                ("pl_rep_fac", ctypes.c_double), ("pl_rep_abs", ctypes.c_double),
+                ("nnlup", ctypes.c_int), ("nplup", ctypes.c_int), ("rep6", ctypes.c_int),
+                ("device", ctypes.c_int), ("graph_steps", ctypes.c_int),
+                ("lanes_per_bead", ctypes.c_int), ("seed", ctypes.c_ulonglong)]
+
+
+class MoleculeDesc(ctypes.Structure):
+    _fields_ = [("nbead", ctypes.c_int),
+                ("nbnd", ctypes.c_int), ("bond_i", ctypes.c_void_p), ("bond_j", ctypes.c_void_p),
+                ("bond_r0", ctypes.c_void_p),
+                ("nang", ctypes.c_int), ("ang_i", ctypes.c_void_p), ("ang_k", ctypes.c_void_p),
+                ("nnat", ctypes.c_int), ("nat_i", ctypes.c_void_p), ("nat_j", ctypes.c_void_p),
+                ("nat_r0", ctypes.c_void_p), ("nat_eps", ctypes.c_void_p),
+                ("nat_eps_energy", ctypes.c_void_p), ("types", ctypes.c_void_p),
+                ("unc_pos", ctypes.c_void_p), ("pos", ctypes.c_void_p), ("vel", ctypes.c_void_p),
+                ("T", ctypes.c_double), ("traj", ctypes.c_uint), ("nsteps", ctypes.c_longlong)]
+
+
+def lib_path() -> str:
+    return os.path.join(_HERE, "libsopgpu.so")
+
+
+def lib() -> ctypes.CDLL:
+    """The engine library; raises if it was not built (no fallback exists)."""
+    global _LIB
+    if _LIB is None:
+        p = lib_path()
+        if not os.path.exists(p):
+            raise RuntimeError(f"{p} is missing: the CUDA engine must be built "
+                               "(python -c 'import __graft_entry__ as g; g.build()')")
+        L = ctypes.CDLL(p)
+        V, I, LL = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong
+        PLL = ctypes.POINTER(LL)
+        sig = {
+            "sop_params_default": (None, [ctypes.POINTER(Params)]),
+            "sop_ctx_create": (I, [ctypes.POINTER(Params), ctypes.POINTER(V)]),
+            "sop_ctx_destroy": (I, [V]),
+            "sop_add_molecule": (I, [V, ctypes.POINTER(MoleculeDesc), ctypes.POINTER(I)]),
+            "sop_commit": (I, [V]),
+            "sop_upload_topology": (I, [V, ctypes.POINTER(MoleculeDesc)]),
+            "sop_upload_state": (I, [V, I, V, V, V]),
+            "sop_step": (I, [V, LL]),
+            "sop_update_neighbor_list": (I, [V, PLL, PLL]),
+            "sop_update_pair_list": (I, [V, PLL, PLL]),
+            "sop_force_eval": (I, [V]),
+            "sop_set_noise": (I, [V, V]),
+            "sop_download": (I, [V, I, V, V, V, V]),
+            "sop_download_list": (I, [V, I, I, LL, V, V, V, PLL]),
+            "sop_energy": (I, [V, I, V]),
+            "sop_observables": (I, [V, I, V]),
+            "sop_molecule_status": (I, [V, I, ctypes.POINTER(I), PLL]),
+            "sop_memory": (I, [V, I, PLL, PLL]),
+            "sop_stream": (I, [V, ctypes.POINTER(V)]),
+            "sop_last_error": (ctypes.c_char_p, [V]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    lib().sop_params_default(ctypes.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+def baseline_params(**kw) -> Params:
+    """The synthetic workloads' settings: absolute 32 A / 16 A list cut-offs,
+    neighbour list every 50 steps, pair list every 10, h = 0.05, zeta = 0.05."""
+    base = dict(h=0.05, zeta=0.05, nl_att_fac=0.0, nl_att_abs=32.0, nl_rep_fac=0.0,
+                nl_rep_abs=32.0, pl_att_fac=0.0, pl_att_abs=16.0, pl_rep_fac=0.0,
+                pl_rep_abs=16.0, nnlup=50, nplup=10)
+    base.update(kw)
+    return default_params(**base)
+
+
+def _p(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+class Engine:
+    """One context: one or more independent molecules on one GPU stream."""
+
+    def __init__(self, params: Params | None = None):
+        self._keep = []
+        self.params = params if params is not None else default_params()
+        h = ctypes.c_void_p()
+        self._check(lib().sop_ctx_create(ctypes.byref(self.params), ctypes.byref(h)), None)
+        self.h = h
+        self.mols: list[Molecule] = []
+
+    def _check(self, rc: int, h) -> None:
+        if rc != SOP_OK:
+            msg = lib().sop_last_error(h)
+            raise SopError(rc, msg.decode() if msg else "")
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().sop_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def add(self, mol: Molecule, xyz: np.ndarray | None = None, T: float = 0.6, traj: int = 0,
+            nsteps: int = -1, vel: np.ndarray | None = None, pos: np.ndarray | None = None,
+            eps_energy: np.ndarray | None = None) -> int:
+        x = np.ascontiguousarray(mol.xyz if xyz is None else xyz, np.float32)
+        arrs = dict(bi=mol.bond_i, bj=mol.bond_j, br=mol.bond_r0, ai=mol.ang_i, ak=mol.ang_k,
+                    ni=mol.nat_i, nj=mol.nat_j, nr=mol.nat_r0, ne=mol.nat_eps, ty=mol.types)
+        a = {k: np.ascontiguousarray(v, np.float32 if k in ("br", "nr", "ne") else np.int32)
+             for k, v in arrs.items()}
+        v = None if vel is None else np.ascontiguousarray(vel, np.float32)
+        ps = None if pos is None else np.ascontiguousarray(pos, np.float32)
+        ee = None if eps_energy is None else np.ascontiguousarray(eps_energy, np.float32)
+        d = MoleculeDesc(mol.n, len(a["bi"]), _p(a["bi"]), _p(a["bj"]), _p(a["br"]),
+                         len(a["ai"]), _p(a["ai"]), _p(a["ak"]), len(a["ni"]), _p(a["ni"]),
+                         _p(a["nj"]), _p(a["nr"]), _p(a["ne"]), _p(ee), _p(a["ty"]), _p(x),
+                         _p(ps), _p(v), float(T), int(traj), int(nsteps))
+        mid = ctypes.c_int()
+        self._check(lib().sop_add_molecule(self.h, ctypes.byref(d), ctypes.byref(mid)), self.h)
+        self.mols.append(mol)
+        return mid.value
+
+    def commit(self) -> None:
+        self._check(lib().sop_commit(self.h), self.h)
+
+    def step(self, n: int) -> None:
+        self._check(lib().sop_step(self.h, int(n)), self.h)
+
+    def force_eval(self) -> None:
+        self._check(lib().sop_force_eval(self.h), self.h)
+
+    def set_noise(self, normals: np.ndarray | None) -> None:
+        if normals is None:
+            self._check(lib().sop_set_noise(self.h, None), self.h)
+        else:
+            z = np.ascontiguousarray(normals, np.float32)
+            self._check(lib().sop_set_noise(self.h, _p(z)), self.h)
+
+    def update_neighbor_list(self) -> tuple[int, int]:
+        a, r = ctypes.c_longlong(), ctypes.c_longlong()
+        self._check(lib().sop_update_neighbor_list(self.h, ctypes.byref(a), ctypes.byref(r)), self.h)
+        return a.value, r.value
+
+    def update_pair_list(self) -> tuple[int, int]:
+        a, r = ctypes.c_longlong(), ctypes.c_longlong()
+        self._check(lib().sop_update_pair_list(self.h, ctypes.byref(a), ctypes.byref(r)), self.h)
+        return a.value, r.value
+
+    def upload_state(self, mol: int, unc_pos, pos=None, vel=None) -> None:
+        u = np.ascontiguousarray(unc_pos, np.float32)
+        p = None if pos is None else np.ascontiguousarray(pos, np.float32)
+        v = None if vel is None else np.ascontiguousarray(vel, np.float32)
+        self._check(lib().sop_upload_state(self.h, mol, _p(p), _p(u), _p(v)), self.h)
+
+    def download(self, mol: int = 0) -> dict:
+        n = self.mols[mol].n
+        out = {k: np.empty((n, 3), np.float32) for k in ("pos", "unc_pos", "vel", "force")}
+        self._check(lib().sop_download(self.h, mol, _p(out["pos"]), _p(out["unc_pos"]),
+                                       _p(out["vel"]), _p(out["force"])), self.h)
+        return out
+
+    def list_pairs(self, mol: int, which: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """(i, j, r0) of a list: 0 att NL, 1 rep NL, 2 att PL, 3 rep PL."""
+        cnt = ctypes.c_longlong()
+        self._check(lib().sop_download_list(self.h, mol, which, 0, None, None, None,
+                                            ctypes.byref(cnt)), self.h)
+        k = cnt.value
+        i, j = np.empty(max(k, 1), np.int32), np.empty(max(k, 1), np.int32)
+        r0 = np.empty(max(k, 1), np.float32)
+        self._check(lib().sop_download_list(self.h, mol, which, k, _p(i), _p(j), _p(r0),
+                                            ctypes.byref(cnt)), self.h)
+        return i[:k], j[:k], r0[:k]
+
+    def energy(self, mol: int = 0) -> np.ndarray:
+        t = np.zeros(5, np.float64)
+        self._check(lib().sop_energy(self.h, mol, _p(t)), self.h)
+        return t
+
+    def observables(self, mol: int = 0) -> dict:
+        o = np.zeros(4, np.float64)
+        self._check(lib().sop_observables(self.h, mol, _p(o)), self.h)
+        return {"Q": o[0], "rgsq": o[1], "kinT": o[2], "contct_nat": int(o[3])}
+
+    def status(self, mol: int = 0) -> tuple[int, int]:
+        st, step = ctypes.c_int(), ctypes.c_longlong()
+        self._check(lib().sop_molecule_status(self.h, mol, ctypes.byref(st), ctypes.byref(step)),
+                    self.h)
+        return st.value, step.value
+
+    def memory(self, mol: int = 0) -> tuple[int, int]:
+        a, b = ctypes.c_longlong(), ctypes.c_longlong()
+        self._check(lib().sop_memory(self.h, mol, ctypes.byref(a), ctypes.byref(b)), self.h)
+        return a.value, b.value
+
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        self._check(lib().sop_stream(self.h, ctypes.byref(s)), self.h)
+        return s.value or 0
+
+
+def plain(mol: Molecule, xyz=None, params: Params | None = None, T: float = 0.6, traj: int = 0,
+          **kw) -> Engine:
+    """The reference's plain path: one molecule in its own context, committed."""
+    e = Engine(params)
+    e.add(mol, xyz, T=T, traj=traj, **kw)
+    e.commit()
+    return e

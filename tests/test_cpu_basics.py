@@ -1,0 +1,129 @@
+"""CPU-side checks: the C-ABI library loads and exports every declared entry
+point, the generator meets the workload specification, Philox matches its
+published known-answer vectors, and the oracle's list filters are consistent."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+from sop_gb300 import engine, system
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "sop_gpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(sop_[a-z_0-9]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(engine.lib_path())
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), s
+
+
+def test_binding_covers_every_declared_symbol():
+    engine.lib()  # binds argtypes for each entry point; raises on a missing one
+    src = open(os.path.join(ROOT, "sop_gb300", "engine.py")).read()
+    for s in declared_symbols():
+        assert f'"{s}"' in src, s
+
+
+def test_params_default_matches_reference():
+    p = engine.default_params()
+    assert (p.k_bnd, p.R0, p.eps_ss, p.sigma_ss, p.eps_rep, p.boxl) == (20.0, 2.0, 1.0, 3.5, 1.0, 500.0)
+    assert (p.h, p.zeta, p.nnlup, p.nplup) == (2.5e-3, 5.0e-2, 50, 1)
+    assert (p.nl_att_fac, p.nl_rep_fac, p.pl_att_fac, p.pl_rep_fac) == (3.2, 3.2, 2.5, 2.5)
+
+
+@pytest.mark.parametrize("n,seed", [(128, 0), (4000, 1)])
+def test_generator_meets_spec(n, seed):
+    m = system.generate(n, seed)
+    x = m.xyz.astype(np.float64)
+    b = np.linalg.norm(x[1:] - x[:-1], axis=1)
+    assert np.abs(b - 3.8).max() < 1e-5
+    u1, u2 = x[:-2] - x[1:-1], x[2:] - x[1:-1]
+    ang = np.degrees(np.arccos((u1 * u2).sum(1) / np.linalg.norm(u1, axis=1) / np.linalg.norm(u2, axis=1)))
+    assert ang.min() >= 80.0 - 1e-3 and ang.max() <= 150.0 + 1e-3
+    R = 3.8 * n ** (1 / 3) * 1.2
+    assert np.linalg.norm(x, axis=1).max() <= R + 1e-4
+    if n <= 4000:
+        d = np.sqrt(((x[:, None, :] - x[None, :, :]) ** 2).sum(-1))
+        iu = np.triu_indices(n, 2)
+        assert d[iu].min() >= 4.0 - 1e-4
+        iu3 = np.triu_indices(n, 3)
+        nat = set(zip(*[a[d[iu3] < 8.0] for a in iu3]))
+        assert nat == set(zip(m.nat_i.tolist(), m.nat_j.tolist()))
+    np.testing.assert_array_equal(m.bond_r0, np.linalg.norm(x[1:] - x[:-1], axis=1).astype(np.float32))
+
+
+def test_generator_is_deterministic_and_seeded():
+    a, b, c = system.generate(500, 7), system.generate(500, 7), system.generate(500, 8)
+    np.testing.assert_array_equal(a.xyz, b.xyz)
+    assert not np.array_equal(a.xyz, c.xyz)
+
+
+def test_per_contact_epsilon_range():
+    m = system.generate(2000, 2, (0.7, 1.3))
+    assert m.nat_eps.min() >= 0.7 and m.nat_eps.max() <= 1.3
+    assert m.nat_eps.std() > 0.1
+
+
+def test_ensemble_and_requests_spec():
+    ns, ts = system.ensemble_spec(512, 60, 1500, 0.5, 0.8, 4)
+    assert ns.min() >= 60 and ns.max() <= 1500 and ts.min() >= 0.5 and ts.max() <= 0.8
+    lg = np.log(ns)
+    assert abs(lg.mean() - 0.5 * (np.log(60) + np.log(1500))) < 0.15
+    r = system.request_stream(200.0, 5.0, seed=5)
+    k = len(r["n"])
+    assert 800 < k < 1200
+    assert r["n"].min() >= 50 and r["n"].max() <= 20000
+    assert r["steps"].min() >= 1e4 and r["steps"].max() <= 1e6
+    assert np.all(np.diff(r["arrival"]) > 0)
+    assert set(np.unique(r["extended"])) == {0, 1}
+
+
+def test_philox_known_answers():
+    """Philox4x32-10 known-answer vectors of the algorithm's reference release."""
+    assert [hex(v) for v in O.philox([0, 0, 0, 0], [0, 0])] == \
+        ["0x6627e8d5", "0xe169c58d", "0xbc57ac4c", "0x9b00dbd8"]
+    assert [hex(v) for v in O.philox([0xffffffff] * 4, [0xffffffff] * 2)] == \
+        ["0x408f276d", "0x41c83b0e", "0xa20bc7c6", "0x6d5451fd"]
+    assert [hex(v) for v in O.philox([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344],
+                                     [0xa4093822, 0x299f31d0])] == \
+        ["0xd16cfe09", "0x94fdcceb", "0x5001e420", "0x24126ea1"]
+
+
+def test_noise_normals_statistics():
+    z = O.noise_normals(20000, 17, 3, 99)
+    assert abs(z.mean()) < 0.02 and abs(z.std() - 1.0) < 0.02
+    z2 = O.noise_normals(20000, 18, 3, 99)
+    assert abs(np.corrcoef(z.ravel(), z2.ravel())[0, 1]) < 0.02
+
+
+def test_oracle_pair_list_is_subset_of_neighbour_list():
+    m = system.generate(600, 3)
+    rng = np.random.default_rng(0)
+    x = (m.xyz + rng.normal(0, 0.5, m.xyz.shape)).astype(np.float32)
+    ni, nj = O.nl_rep(m, x, 3.2, 0.0)
+    pi, pj = O.filter_rep(m, x, ni, nj, 2.5, 0.0)
+    s_nl = set(zip(ni.tolist(), nj.tolist()))
+    s_pl = set(zip(pi.tolist(), pj.tolist()))
+    assert s_pl <= s_nl and len(s_pl) > 0
+    nat = set(zip(m.nat_i.tolist(), m.nat_j.tolist()))
+    assert not (s_nl & nat)
+    assert all(j - i > 2 for i, j in s_nl)
+
+
+def test_rcut_matches_reference_rounding():
+    # rcut = 3.2 * r0 in double rounded to FP32, squared in FP32 (sop.cu:746-747)
+    r0 = np.float32(5.123456)
+    rc = np.float32(3.2 * np.float64(r0))
+    assert O.lib().orc_rcut2(3.2, 0.0, r0) == np.float32(rc * rc)
+    assert O.lib().orc_rcut2(0.0, 32.0, r0) == np.float32(1024.0)

@@ -1,0 +1,274 @@
+"""GPU parity of the plain path against the oracle (through the C ABI).
+
+Lists: bit-exact as sets (the engine's FP32 predicate is the reference's host
+filter).  Forces: max relative error <= 1e-5 against FP64 on the same FP32
+coordinates and lists (per-bead |dF| / |F|, |F| floored at 1e-3 of the RMS
+bead force).  Single steps: identical injected noise.
+"""
+import numpy as np
+import pytest
+
+from helpers import att_sel, force_error, oracle_lists, pairset
+from oracle import pyoracle as O
+from sop_gb300 import engine, system
+
+pytestmark = pytest.mark.gpu
+
+FORCE_TOL = 1e-5
+
+_MOLS = {}
+
+
+def mol_of(n, seed, eps_range=None):
+    key = (n, seed, eps_range)
+    if key not in _MOLS:
+        _MOLS[key] = system.generate(n, seed, eps_range)
+    return _MOLS[key]
+
+
+def perturbed(mol, sigma, seed=0):
+    rng = np.random.default_rng(seed)
+    return (mol.xyz + rng.normal(0.0, sigma, mol.xyz.shape)).astype(np.float32)
+
+
+def params(mode, **kw):
+    if mode == "factor":
+        return engine.default_params(h=0.05, zeta=0.05, **kw)
+    return engine.baseline_params(**kw)
+
+
+def gpu_lists(e, mol):
+    ai, aj, ar = e.list_pairs(0, 0)
+    ri, rj, _ = e.list_pairs(0, 1)
+    pai, paj, par = e.list_pairs(0, 2)
+    pri, prj, _ = e.list_pairs(0, 3)
+    return (ai, aj, ar), (ri, rj), (pai, paj, par), (pri, prj)
+
+
+@pytest.mark.parametrize("n,seed", [(128, 0), (4000, 1)])
+@pytest.mark.parametrize("mode", ["factor", "absolute"])
+@pytest.mark.parametrize("sigma", [0.0, 0.4])
+def test_lists_bit_exact(n, seed, mode, sigma):
+    mol = mol_of(n, seed)
+    x = perturbed(mol, sigma, seed + 7)
+    p = params(mode)
+    with engine.plain(mol, x, p) as e:
+        (ai, aj, ar), (ri, rj), (pai, paj, par), (pri, prj) = gpu_lists(e, mol)
+    nl_att, (nri, nrj), pl_att, (opi, opj) = oracle_lists(mol, x, p)
+    assert pairset(ai, aj) == pairset(mol.nat_i[nl_att], mol.nat_j[nl_att])
+    assert pairset(ri, rj) == pairset(nri, nrj)
+    assert pairset(pai, paj) == pairset(mol.nat_i[pl_att], mol.nat_j[pl_att])
+    assert pairset(pri, prj) == pairset(opi, opj)
+    # the attractive entries carry their native distance unchanged
+    sel = att_sel(mol, pai, paj)
+    np.testing.assert_array_equal(par, mol.nat_r0[sel])
+    assert len(pri) > 0
+
+
+@pytest.mark.parametrize("n,seed", [(128, 0), (4000, 1)])
+@pytest.mark.parametrize("mode", ["factor", "absolute"])
+@pytest.mark.parametrize("sigma", [0.0, 0.25])
+def test_forces_vs_fp64(n, seed, mode, sigma):
+    # sigma (A per axis) keeps every bond well inside the FENE range |r - r0| < R0;
+    # a larger perturbation breaks bonds, where the force is undefined and the
+    # engine stops the molecule (tested in test_fene_range_is_flagged).
+    mol = mol_of(n, seed)
+    x = perturbed(mol, sigma, seed + 11)
+    with engine.plain(mol, x, params(mode)) as e:
+        e.set_noise(np.zeros((mol.n, 3), np.float32))
+        e.force_eval()
+        assert e.status(0)[0] == 0
+        f = e.download()["force"]
+        pai, paj, _ = e.list_pairs(0, 2)
+        pri, prj, _ = e.list_pairs(0, 3)
+    fo, _ = O.forces_f64(mol, x, att_sel(mol, pai, paj), pri, prj)
+    err = force_error(f, fo)
+    assert err <= FORCE_TOL, err
+
+
+def test_forces_per_contact_epsilon():
+    mol = mol_of(4000, 2, (0.7, 1.3))
+    x = perturbed(mol, 0.3, 5)
+    with engine.plain(mol, x, params("absolute")) as e:
+        e.set_noise(np.zeros((mol.n, 3), np.float32))
+        e.force_eval()
+        f = e.download()["force"]
+        pai, paj, _ = e.list_pairs(0, 2)
+        pri, prj, _ = e.list_pairs(0, 3)
+    fo, _ = O.forces_f64(mol, x, att_sel(mol, pai, paj), pri, prj)
+    assert force_error(f, fo) <= FORCE_TOL
+
+
+@pytest.mark.parametrize("mode", ["factor", "absolute"])
+def test_energy_vs_fp64(mode):
+    mol = mol_of(4000, 1)
+    x = perturbed(mol, 0.3, 3)
+    with engine.plain(mol, x, params(mode)) as e:
+        t = e.energy()
+        pai, paj, _ = e.list_pairs(0, 2)
+        pri, prj, _ = e.list_pairs(0, 3)
+    _, eo = O.forces_f64(mol, x, att_sel(mol, pai, paj), pri, prj)
+    np.testing.assert_allclose(t[:4], eo, rtol=2e-5, atol=1e-6)
+    np.testing.assert_allclose(t[4], eo.sum(), rtol=2e-5)
+
+
+def test_observables_vs_fp64():
+    mol = mol_of(4000, 1)
+    x = perturbed(mol, 1.0, 4)
+    rng = np.random.default_rng(9)
+    v = rng.normal(0, 0.8, x.shape).astype(np.float32)
+    with engine.plain(mol, x, params("absolute"), vel=v) as e:
+        ob = e.observables()
+    oo = O.observables(mol, x, v)
+    assert ob["contct_nat"] == oo["contct_nat"]
+    assert ob["Q"] == pytest.approx(oo["Q"], abs=1e-12)
+    assert ob["rgsq"] == pytest.approx(oo["rgsq"], rel=1e-9)
+    assert ob["kinT"] == pytest.approx(oo["kinT"], rel=1e-9)
+
+
+def test_philox_noise_matches_oracle():
+    mol = mol_of(4000, 1)
+    T, traj = 0.7, 3
+    p = params("absolute", seed=0x1234_5678_9ABC)
+    with engine.plain(mol, mol.xyz, p, T=T, traj=traj) as e:
+        e.set_noise(np.zeros((mol.n, 3), np.float32))
+        e.force_eval()
+        f0 = e.download()["force"].astype(np.float64)
+        e.set_noise(None)
+        e.force_eval()
+        f1 = e.download()["force"].astype(np.float64)
+    sig = O.langevin_consts(0.05, 0.05, T)[4]
+    z = (f1 - f0) / sig
+    zo = O.noise_normals(mol.n, 0, traj, 0x1234_5678_9ABC)
+    np.testing.assert_allclose(z, zo, atol=2e-5)
+    assert abs(z.mean()) < 0.05 and abs(z.std() - 1.0) < 0.05
+
+
+def _oracle_steps(mol, x0, v0, z, T, h, zeta, nsteps, p, boxl=500.0):
+    """FP64 oracle trajectory with the engine's cadence and the same injected
+    normals z every step; lists from the FP32 positions as the engine keeps them."""
+    c = O.langevin_consts(h, zeta, T)
+    x = x0.astype(np.float64)
+    pos = x.copy()
+    v = v0.astype(np.float64)
+    xf = x0.astype(np.float32)
+    nl = oracle_lists(mol, xf, p, boxl)
+    nl_att, (nri, nrj) = nl[0], nl[1]
+    pl_att, (pri, prj) = nl[2], nl[3]
+    f, _ = O.forces_f64(mol, xf, pl_att, pri, prj)
+    f += c[4] * z
+    incr = np.zeros_like(x)
+    for n in range(1, nsteps + 1):
+        if n % p.nnlup == 0:
+            nl_att = O.filter_att(mol, xf, None, p.nl_att_fac, p.nl_att_abs, boxl)
+            nri, nrj = O.nl_rep(mol, xf, p.nl_rep_fac, p.nl_rep_abs, boxl)
+        if n % p.nnlup == 0 or p.nplup <= 1 or n % p.nplup == 0:
+            pl_att = O.filter_att(mol, xf, nl_att, p.pl_att_fac, p.pl_att_abs, boxl)
+            pri, prj = O.filter_rep(mol, xf, nri, nrj, p.pl_rep_fac, p.pl_rep_abs, boxl)
+        incr = c[0] * v + c[1] * f
+        x = x + incr
+        pos = pos + incr
+        pos -= boxl * np.rint(pos / boxl)
+        xf = x.astype(np.float32)
+        f, _ = O.forces_f64(mol, xf, pl_att, pri, prj)
+        f += c[4] * z
+        v = c[2] * incr + c[3] * f
+    return x, v, f
+
+
+@pytest.mark.parametrize("mode,nsteps", [("factor", 1), ("absolute", 1), ("factor", 12)])
+def test_steps_with_injected_noise(mode, nsteps):
+    mol = mol_of(128, 0)
+    x0 = perturbed(mol, 0.2, 1)
+    rng = np.random.default_rng(2)
+    v0 = rng.normal(0, 0.5, x0.shape).astype(np.float32)
+    z = rng.normal(0, 1, x0.shape).astype(np.float32)
+    T = 0.6
+    p = params(mode, nnlup=5, nplup=1 if mode == "factor" else 2)
+    with engine.plain(mol, x0, p, T=T, vel=v0) as e:
+        e.set_noise(z)
+        e.force_eval()
+        e.step(nsteps)
+        st = e.download()
+        assert e.status(0) == (0, nsteps)
+    x, v, f = _oracle_steps(mol, x0, v0, z.astype(np.float64), T, 0.05, 0.05, nsteps, p)
+    assert force_error(st["force"], f) <= (FORCE_TOL if nsteps == 1 else 1e-4)
+    np.testing.assert_allclose(st["unc_pos"], x, atol=5e-5 * nsteps)
+    np.testing.assert_allclose(st["vel"], v, atol=2e-4 * nsteps, rtol=1e-4)
+
+
+def test_deterministic_and_graph_equals_eager():
+    mol = mol_of(4000, 1)
+    outs = []
+    for gs in (10, 10, 4):
+        p = engine.baseline_params(graph_steps=gs)
+        with engine.plain(mol, mol.xyz, p, T=0.6, traj=1) as e:
+            e.step(3)   # eager partial block
+            e.step(57)  # graph replays + an eager tail
+            outs.append(e.download())
+    for k in ("unc_pos", "vel", "force", "pos"):
+        np.testing.assert_array_equal(outs[0][k], outs[1][k])
+        np.testing.assert_array_equal(outs[0][k], outs[2][k])
+
+
+@pytest.mark.parametrize("boxl", [40000.0, 500.0])
+def test_extended_chain_lists(boxl):
+    """Extended start: with a large box the cell grid is a long row; with the
+    reference's 500 A box the chain wraps, the minimum image matters and the
+    all-pairs scan is used."""
+    mol = mol_of(1500, 3)
+    x = mol.extended_xyz()
+    p = params("absolute", boxl=boxl)
+    with engine.plain(mol, x, p) as e:
+        _, (ri, rj), _, (pri, prj) = gpu_lists(e, mol)
+    _, (nri, nrj), _, (opi, opj) = oracle_lists(mol, x, p, boxl)
+    assert pairset(ri, rj) == pairset(nri, nrj)
+    assert pairset(pri, prj) == pairset(opi, opj)
+
+
+def test_batched_equals_alone():
+    """Molecules packed into one context give bit-identical results to the
+    same molecules run alone."""
+    sizes = [(90, 10), (700, 11), (1500, 12)]
+    mols = [mol_of(n, s) for n, s in sizes]
+    p = engine.baseline_params()
+    alone = []
+    for k, m in enumerate(mols):
+        with engine.plain(m, m.xyz, p, T=0.5 + 0.1 * k, traj=k) as e:
+            e.step(40)
+            alone.append(e.download())
+    with engine.Engine(p) as e:
+        for k, m in enumerate(mols):
+            e.add(m, m.xyz, T=0.5 + 0.1 * k, traj=k)
+        e.commit()
+        e.step(40)
+        for k in range(len(mols)):
+            d = e.download(k)
+            for key in ("unc_pos", "vel", "force"):
+                np.testing.assert_array_equal(d[key], alone[k][key])
+
+
+def test_fene_range_is_flagged():
+    """A bond stretched beyond R0 stops the molecule with a status bit instead
+    of producing log of a negative number (energy.cu:220 has no guard)."""
+    mol = mol_of(128, 0)
+    x = mol.xyz.copy()
+    x[64:] += np.array([3.0, 0.0, 0.0], np.float32)   # bond 63-64 stretched by ~3 A
+    with engine.plain(mol, x, engine.baseline_params()) as e:
+        st, n = e.status(0)
+        assert st & engine.MOL_FENE_RANGE
+        e.step(10)
+        assert e.status(0)[1] == 0   # the molecule no longer advances
+
+
+def test_long_run_stays_folded():
+    mol = mol_of(128, 0)
+    with engine.plain(mol, mol.xyz, engine.baseline_params(), T=0.6) as e:
+        e.step(2000)
+        st, n = e.status(0)
+        ob = e.observables()
+        en = e.energy()
+    assert st == 0 and n == 2000
+    assert np.all(np.isfinite(en))
+    assert ob["Q"] > 0.6
+    assert 0.2 < ob["kinT"] < 1.2
