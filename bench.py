@@ -1,0 +1,422 @@
+#!/usr/bin/env python3
+"""Aggregate bead-steps/s of the batched SOP engine on GB300.
+
+Workload (default): the batched ensemble -- 512 independent trajectories, N
+log-uniform in [60, 1500] beads (structure seed = trajectory index), kBT
+uniform in [0.5, 0.8] kcal/mol, a Philox stream each, FP32, k = 20, R0 = 2,
+eps = 1, sigma = 3.8, neighbour list 32 A every 50 steps, pair list 16 A every
+10 steps, h = 0.05, zeta = 0.05, started from the native structures.  The step
+loop runs as a CUDA graph of 10 steps per replay; one bench step is one replay
+(10 Langevin steps of every trajectory).  Inputs are the project's seeded
+synthetic structures.
+
+Timing: W untimed bench steps, then K bench steps, each bracketed by CUDA
+events on the engine's stream, with a 256 MiB write (flushes the 129 MB L2)
+before every step outside the events; a barrier and synchronize on both sides;
+the max over ranks.  Under torchrun each rank runs its own 512-trajectory
+ensemble (replicas: trajectories are independent, no collective), so the
+scaling is weak.
+
+`--impl reference` times the reference's algorithm on the host cores (the
+serial FP32 CPU restatement of its host routines and kernels, all threads,
+one molecule per thread) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from sop_gb300 import system  # noqa: E402
+
+METRIC = "aggregate bead-steps/s (batched ensemble)"
+UNIT = "bead-steps/s"
+N_TRAJ = 512
+MD_STEPS = 10
+CUT = [0.0, 32.0, 0.0, 32.0, 0.0, 16.0, 0.0, 16.0]   # absolute NL / PL cut-offs (A)
+
+
+def workload_config(total_beads: int) -> dict:
+    return {
+        "workload": "batched ensemble: 512 trajectories, N log-uniform [60,1500] (seed = index), "
+                    "kBT U[0.5,0.8], FP32, NL 32 A / 50 steps, PL 16 A / 10 steps, h = 0.05, "
+                    "zeta = 0.05, CUDA graph of 10 steps per replay",
+        "trajectories": N_TRAJ,
+        "beads_per_replica": int(total_beads),
+        "md_steps_per_bench_step": MD_STEPS,
+        "l2": "flushed before every timed step (256 MiB write); working set exceeds L2 only for the lists",
+    }
+
+
+def ensemble(rank: int):
+    ns, ts = system.ensemble_spec(N_TRAJ, 60, 1500, 0.5, 0.8, seed=4)
+    mols = [system.generate(int(n), rank * N_TRAJ + k) for k, n in enumerate(ns)]
+    return mols, ts
+
+
+def measured_peaks() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic() -> float | None:
+    """DRAM bytes per launch of the step kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "step_kernel_ensemble.md")
+    try:
+        for line in open(p):
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            time.sleep(0.3)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in getattr(self, "out", "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def launches_per_bench_step(p, s0: int) -> int:
+    """Kernels of the engine in one replay starting after step s0."""
+    nl_kernels = 11    # bbox reset, bbox, grid, grid base, assign, 3 scan, scatter, cellsort, nl
+    n = 0
+    for k in range(MD_STEPS):
+        st = s0 + 1 + k
+        nl = p.nnlup > 0 and st % p.nnlup == 0
+        pl = nl or p.nplup <= 1 or st % p.nplup == 0
+        n += (nl_kernels if nl else 0) + (1 if pl else 0) + 1
+    return n + 1   # step advance
+
+
+def step_kernel_bytes(e, mols) -> tuple[float, dict]:
+    """Algorithmic bytes of one launch of the fused step kernel:
+    80 N (Langevin: read x, v, f; write x, v as float4) + 32 N (read x, write f)
+    + 4 B (bond r0) + 4 P_rep + 8 P_att (+4 P_att for per-contact epsilon)."""
+    ls = e.list_sizes()
+    N = sum(m.n for m in mols)
+    B = sum(len(m.bond_i) for m in mols)
+    byts = 112.0 * N + 4.0 * B + 4.0 * ls["nil_rep"] + 12.0 * ls["nil_att"]
+    return byts, ls
+
+
+def cpu_baseline(mols, ts, seconds_target: float = 15.0) -> dict:
+    """The reference algorithm on the host cores (one molecule per thread)."""
+    from oracle import pyoracle as O
+    cores = os.cpu_count() or 1
+    runs = [O.RefRun(m, m.xyz, CUT, 0.05, 0.05, float(t), 50, 10, 1234, k)
+            for k, (m, t) in enumerate(zip(mols, ts))]
+    # initial lists and forces (step 0) outside the timing
+    with ThreadPoolExecutor(cores) as ex:
+        list(ex.map(lambda r: r.advance(0), runs))
+    beads = sum(m.n for m in mols)
+    steps = 10
+    groups = [runs[c::cores] for c in range(cores)]
+
+    def work(g, k):
+        for r in g:
+            r.advance(k)
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(cores) as ex:
+        list(ex.map(lambda g: work(g, steps), groups))
+    dt = time.perf_counter() - t0
+    # scale the sample to about `seconds_target` of wall time
+    more = max(0, int(steps * (seconds_target / max(dt, 1e-3) - 1.0)))
+    more = min(more, 400)
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(cores) as ex:
+        list(ex.map(lambda g: work(g, more), groups))
+    dt2 = time.perf_counter() - t0 if more else 0.0
+    tot_steps = steps + more
+    tot_t = dt + dt2
+    for r in runs:
+        r.close()
+    return {"value": beads * tot_steps / tot_t, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"all {len(mols)} trajectories ({beads} beads), {tot_steps} Langevin steps "
+                      f"each, serial FP32 restatement of the reference's host list filters, "
+                      f"force kernels and integrator, one trajectory per thread"}
+
+
+def run_reference(args, rank: int) -> None:
+    from oracle import pyoracle as O
+    mols, ts = ensemble(0)
+    cores = os.cpu_count() or 1
+    runs = [O.RefRun(m, m.xyz, CUT, 0.05, 0.05, float(t), 50, 10, 1234, k)
+            for k, (m, t) in enumerate(zip(mols, ts))]
+    beads = np.array([m.n for m in mols])
+    # one reference step: one Langevin step of a rotating sample of 64 trajectories
+    sample = 64
+    order = np.arange(len(runs))
+    with ThreadPoolExecutor(cores) as ex:
+        list(ex.map(lambda r: r.advance(0), runs))
+
+        def one(step_idx):
+            sel = order[(step_idx * sample) % len(runs):][:sample]
+            if len(sel) < sample:
+                sel = np.concatenate([sel, order[:sample - len(sel)]])
+            groups = [sel[c::cores] for c in range(cores)]
+            list(ex.map(lambda g: [runs[k].advance(1) for k in g], groups))
+            return int(beads[sel].sum())
+
+        for w in range(args.warmup):
+            one(w)
+        t0 = time.perf_counter()
+        done = 0
+        for k in range(args.steps):
+            done += one(args.warmup + k)
+        dt = time.perf_counter() - t0
+    val = done / dt
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": workload_config(int(beads.sum())),
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"each step: one Langevin step of {sample} of the 512 "
+                                       f"trajectories (rotating), serial FP32 restatement of the "
+                                       f"reference algorithm, {cores} threads"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-loop comparison")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args, rank)
+        return
+
+    import torch
+    import torch.distributed as dist
+    from sop_gb300 import engine
+
+    if world > 1:
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    mols, ts = ensemble(rank)
+    total = sum(m.n for m in mols)
+    p = engine.baseline_params(device=local, graph_steps=MD_STEPS)
+    e = engine.Engine(p)
+    for k, (m, t) in enumerate(zip(mols, ts)):
+        e.add(m, m.xyz, T=float(t), traj=rank * N_TRAJ + k)
+    e.commit()
+    stream = torch.cuda.ExternalStream(e.stream(), device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    for _ in range(args.warmup):
+        e.step_async(MD_STEPS)
+    e.sync()
+    s_start = e.status(0)[1]
+
+    K = args.steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(K)]
+    barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            for k in range(K):
+                flush.zero_()
+                ev[k][0].record(stream)
+                e.step_async(MD_STEPS)
+                ev[k][1].record(stream)
+        torch.cuda.synchronize(dev)
+        e.sync()
+    barrier()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    s_end = e.status(0)[1]
+    if s_end - s_start != K * MD_STEPS:
+        raise RuntimeError("a neighbour-list overflow re-ran steps outside the timed region")
+    statuses = [e.status(m)[0] for m in range(len(mols))]
+    t_local = sum(ms) / 1e3
+    t_max = t_local
+    if world > 1:
+        tt = torch.tensor([t_local], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = world * total * MD_STEPS * K / t_max
+
+    # ---- roofline of the dominant kernel (the fused step kernel), timed alone
+    byts, ls = step_kernel_bytes(e, mols)
+    reps = 50
+    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(reps)]
+    with torch.cuda.stream(stream):
+        for k in range(reps):
+            flush.zero_()
+            kev[k][0].record(stream)
+            e.launch_stage(0, 0)
+            kev[k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    t_kernel = statistics.median(a.elapsed_time(b) for a, b in kev) / 1e3
+    peak, peak_kind = measured_peaks()
+    achieved = byts / t_kernel / 1e9
+    traffic = profile_traffic()
+    e.close()
+
+    # ---- end to end through the C ABI: host arrays in, coordinates out every step
+    e2e = None
+    if not args.no_e2e:
+        K2 = max(10, min(K, 500))
+        pinned = torch.empty((total, 3), dtype=torch.float32, pin_memory=True).numpy()
+        h2d = 0
+        for m in mols:
+            h2d += 12 * m.n * 2 + 12 * len(m.bond_i) + 8 * len(m.ang_i) + 16 * len(m.nat_i) + 4 * m.n
+        barrier()
+        t0 = time.perf_counter()
+        e2 = engine.Engine(p)
+        for k, (m, t) in enumerate(zip(mols, ts)):
+            e2.add(m, m.xyz, T=float(t), traj=rank * N_TRAJ + k)
+        e2.commit()
+        for _ in range(K2):
+            e2.step(MD_STEPS)
+            e2.download_all(pinned)
+        dt = time.perf_counter() - t0
+        e2.close()
+        barrier()
+        if world > 1:
+            tt = torch.tensor([dt], device=dev, dtype=torch.float64)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            dt = float(tt.item())
+        e2e = {"value": world * total * MD_STEPS * K2 / dt, "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d / K2), "d2h_bytes_per_step": int(12 * total),
+               "steps": K2, "note": "wall clock: context creation, upload of every structure from "
+                                     "host arrays, set-up, then per step 10 Langevin steps and a "
+                                     "download of every coordinate"}
+
+    cpu = None
+    plain = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(mols, ts)
+    if rank == 0 and not args.no_plain:
+        # the plain path looping over the same trajectories: one context each
+        sample = list(range(0, len(mols), 8))
+        nst = 200
+        beads = 0
+        t_plain = 0.0
+        for k in sample:
+            m = mols[k]
+            ep = engine.plain(m, m.xyz, engine.baseline_params(device=local, graph_steps=MD_STEPS),
+                              T=float(ts[k]), traj=k)
+            ep.step(MD_STEPS)
+            t0 = time.perf_counter()
+            ep.step(nst)
+            t_plain += time.perf_counter() - t0
+            beads += m.n
+            ep.close()
+        plain = {"value": beads * nst / t_plain, "unit": UNIT,
+                 "sample": f"{len(sample)} of the trajectories (every 8th), {nst} steps each, "
+                           f"one plain context at a time (the reference's single-molecule loop)"}
+
+    if rank == 0:
+        n_launch = sum(launches_per_bench_step(p, s_start + k * MD_STEPS) for k in range(K))
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / K, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(total),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "fused force + Langevin step (k_step)",
+                         "bytes_per_launch": byts, "launch_us": t_kernel * 1e6,
+                         "peak_source": peak_kind},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": int(n_launch),
+            "clocks": clk.summary(),
+            "plain_loop": plain,
+            "batched_over_plain": (value / world / plain["value"]) if plain else None,
+            "lists": ls,
+            "molecule_errors": int(sum(1 for s in statuses if s & 3)),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -137,6 +137,27 @@ int sop_upload_state(void* ctx, int mol, const float* pos, const float* unc_pos,
  */
 int sop_step(void* ctx, long long nsteps);
 
+/*
+ * sop_step without the final wait: queues nsteps steps on the context's
+ * stream and returns.  A neighbour-list overflow during the queued work
+ * freezes every molecule at the start of the block that overflowed;
+ * sop_sync regrows the lists and re-runs the frozen steps.  Together they
+ * are sop_step; apart they let a caller overlap host work or time the device
+ * work alone.  The reference's loop always waits (cudaThreadSynchronize,
+ * energy.cu:148).
+ */
+int sop_step_async(void* ctx, long long nsteps);
+int sop_sync(void* ctx);
+
+/*
+ * Queues one stage of the step loop at block offset koff, for timing and
+ * profiling: 0 the fused force + Langevin step kernel, 1 the pair-list
+ * rebuild, 2 the neighbour-list rebuild, 3 the end-of-block step advance
+ * (count = koff).  Stages launched out of the loop's order leave the
+ * trajectory undefined; the loop itself is sop_step.
+ */
+int sop_launch_stage(void* ctx, int stage, int koff);
+
 /* Rebuilds the neighbour lists now (update_neighbor_list, sop.cu:928-1262);
  * returns the attractive / repulsive totals over all molecules (pairs, each
  * counted once) when the pointers are non-NULL. */
@@ -172,6 +193,15 @@ int sop_download(void* ctx, int mol, float* pos, float* unc_pos, float* vel, flo
  */
 int sop_download_list(void* ctx, int mol, int which, long long cap, int* i_out, int* j_out,
                       float* r0_out, long long* count);
+
+/* Current list sizes over all molecules, each pair counted once:
+ * out[0..3] = attractive NL, repulsive NL, attractive PL, repulsive PL
+ * (the reference's nnl_att, nnl_rep, nil_att, nil_rep globals). */
+int sop_list_sizes(void* ctx, long long* out);
+
+/* Current unwrapped coordinates of every molecule, molecules in id order,
+ * 3 floats per bead, into one host array (one device-to-host copy). */
+int sop_download_all(void* ctx, float* unc_pos);
 
 /*
  * Energy terms of molecule `mol` on its current pair lists (energy_eval and

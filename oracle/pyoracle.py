@@ -42,7 +42,6 @@ def lib() -> ctypes.CDLL:
         L = ctypes.CDLL(path)
         L.orc_nl_rep.restype = ctypes.c_longlong
         L.orc_filter_rep.restype = ctypes.c_longlong
-        L.orc_ref_run_f32.restype = ctypes.c_longlong
         L.orc_rcut2.restype = ctypes.c_float
         L.orc_rcut2.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_float]
         _LIB = L
@@ -151,19 +150,49 @@ def observables(mol, x, v=None, boxl=500.0):
     return {"Q": out[0], "rgsq": out[1], "kinT": out[2], "contct_nat": int(out[3])}
 
 
-def ref_run_f32(mol, unc, pos, vel, cut, h, zeta, T, nnlup, nplup, seed, traj, nsteps,
-                params=None):
-    """The serial FP32 CPU baseline (reference algorithm).  Updates unc/pos/vel in place."""
-    for a in (unc, pos, vel):
-        assert a.dtype == np.float32 and a.flags.c_contiguous
-    cut = np.ascontiguousarray(cut, np.float64)
-    return lib().orc_ref_run_f32(
-        mol.n, _p(unc), _p(pos), _p(vel), _p(_i32(mol.types)), len(mol.bond_i),
-        _p(_i32(mol.bond_i)), _p(_i32(mol.bond_j)), _p(_f32(mol.bond_r0)), len(mol.ang_i),
-        _p(_i32(mol.ang_i)), _p(_i32(mol.ang_k)), len(mol.nat_i), _p(_i32(mol.nat_i)),
-        _p(_i32(mol.nat_j)), _p(_f32(mol.nat_r0)), _p(_f32(mol.nat_eps)),
-        _p(params_array(params)), _p(cut), D(h), D(zeta), D(T), nnlup, nplup,
-        ctypes.c_ulonglong(seed), ctypes.c_uint(traj), LL(nsteps))
+class RefRun:
+    """The serial FP32 CPU baseline of one molecule (the reference's algorithm,
+    orc_ref_* in sop_oracle.c); state persists between advance() calls.
+    cut = [nl_att_fac, nl_att_abs, nl_rep_fac, nl_rep_abs, pl_att_fac, ...]."""
+
+    def __init__(self, mol, unc, cut, h, zeta, T, nnlup, nplup, seed, traj, vel=None,
+                 pos=None, params=None):
+        L = lib()
+        L.orc_ref_create.restype = ctypes.c_void_p
+        L.orc_ref_advance.restype = ctypes.c_longlong
+        L.orc_ref_advance.argtypes = [ctypes.c_void_p, ctypes.c_longlong]
+        L.orc_ref_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_ref_state.argtypes = [ctypes.c_void_p] * 4
+        self.n = mol.n
+        keep = [_f32(unc), None if pos is None else _f32(pos), None if vel is None else _f32(vel),
+                _i32(mol.types), _i32(mol.bond_i), _i32(mol.bond_j), _f32(mol.bond_r0),
+                _i32(mol.ang_i), _i32(mol.ang_k), _i32(mol.nat_i), _i32(mol.nat_j),
+                _f32(mol.nat_r0), _f32(mol.nat_eps), params_array(params),
+                np.ascontiguousarray(cut, np.float64)]
+        u, p, v, ty, bi, bj, br, ai, ak, ni, nj, nr, ne, pa, cu = keep
+        self.h = L.orc_ref_create(
+            mol.n, _p(u), _p(p), _p(v), _p(ty), len(bi), _p(bi), _p(bj), _p(br), len(ai),
+            _p(ai), _p(ak), len(ni), _p(ni), _p(nj), _p(nr), _p(ne), _p(pa), _p(cu), D(h),
+            D(zeta), D(T), nnlup, nplup, ctypes.c_ulonglong(seed), ctypes.c_uint(traj))
+        if not self.h:
+            raise MemoryError("orc_ref_create failed")
+
+    def advance(self, nsteps: int) -> None:
+        if lib().orc_ref_advance(self.h, nsteps) < 0:
+            raise RuntimeError("orc_ref_advance failed")
+
+    def state(self):
+        out = [np.empty((self.n, 3), np.float32) for _ in range(3)]
+        lib().orc_ref_state(self.h, *[_p(a) for a in out])
+        return {"unc_pos": out[0], "pos": out[1], "vel": out[2]}
+
+    def close(self):
+        if self.h:
+            lib().orc_ref_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 # ------------------------------------------------------ reference host routines

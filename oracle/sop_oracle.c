@@ -358,144 +358,226 @@ long long orc_filter_rep(const float* x, const int* type, long long ncand, const
  * (energy.cu:228-584), the noise force, and the two integrator kernels
  * (sop.cu:421-462).  Noise comes from the engine's Philox stream (the
  * reference's cuRAND XORWOW is a different generator; the cost of drawing
- * normals is comparable).  State arrays are 3n floats, updated in place.
- * The list cut-off factors are cut[0..3] = att_fac, att_abs, rep_fac, rep_abs
- * for the neighbour list and cut[4..7] for the pair list.
- * Returns the number of steps run, or -1 on allocation failure.
+ * normals is comparable).  The list cut-offs are cut[0..3] = att_fac,
+ * att_abs, rep_fac, rep_abs for the neighbour list and cut[4..7] for the
+ * pair list.  The state persists between orc_ref_advance calls.
  */
-long long orc_ref_run_f32(int n, float* unc, float* pos, float* vel, const int* type, int nbnd,
-                          const int* bi, const int* bj, const float* br0, int nang,
-                          const int* ai, const int* ak, int nnat, const int* ni, const int* nj,
-                          const float* nr0, const float* neps, const double* params,
-                          const double* cut, double h, double zeta, double T, int nnlup,
-                          int nplup, unsigned long long seed, unsigned int traj,
-                          long long nsteps) {
-  const float boxl = (float)params[P_BOXL];
-  const float k_bnd = (float)params[P_KBND];
-  const float R0sq = (float)(params[P_R0] * params[P_R0]);
-  const float f_ang = (float)(6.0 * params[P_EPS_SS] * pow(params[P_SIG_SS], 6.0));
-  const float eps_rep = (float)params[P_EPS_REP];
+typedef struct orc_ref {
+  int n, nbnd, nang, nnat, nnlup, nplup;
+  float *unc, *pos, *vel, *frc, *incr, *br0, *nr0, *neps;
+  int *type, *bi, *bj, *ai, *ak, *ni, *nj;
+  double params[P_NPARAM], cut[8];
+  float a1, a2, a3, a4, var;
+  int *nl_att, *pl_att, nnl_att, nil_att;
+  int *nli, *nlj, *pli, *plj;
+  long long nnl_rep, nil_rep, cap, step;
+  uint32_t key[2];
+  unsigned traj;
+} orc_ref;
+
+static void* dupmem(const void* src, size_t bytes) {
+  void* p = malloc(bytes ? bytes : 1);
+  if (p && src && bytes) memcpy(p, src, bytes);
+  return p;
+}
+
+void orc_ref_destroy(orc_ref* r) {
+  if (!r) return;
+  free(r->unc); free(r->pos); free(r->vel); free(r->frc); free(r->incr);
+  free(r->br0); free(r->nr0); free(r->neps); free(r->type); free(r->bi); free(r->bj);
+  free(r->ai); free(r->ak); free(r->ni); free(r->nj); free(r->nl_att); free(r->pl_att);
+  free(r->nli); free(r->nlj); free(r->pli); free(r->plj);
+  free(r);
+}
+
+orc_ref* orc_ref_create(int n, const float* unc, const float* pos, const float* vel,
+                        const int* type, int nbnd, const int* bi, const int* bj,
+                        const float* br0, int nang, const int* ai, const int* ak, int nnat,
+                        const int* ni, const int* nj, const float* nr0, const float* neps,
+                        const double* params, const double* cut, double h, double zeta,
+                        double T, int nnlup, int nplup, unsigned long long seed,
+                        unsigned int traj) {
+  orc_ref* r = (orc_ref*)calloc(1, sizeof(orc_ref));
+  if (!r) return NULL;
+  size_t f3 = sizeof(float) * 3 * (size_t)n;
+  r->n = n; r->nbnd = nbnd; r->nang = nang; r->nnat = nnat; r->nnlup = nnlup; r->nplup = nplup;
+  r->unc = (float*)dupmem(unc, f3);
+  r->pos = (float*)dupmem(pos ? pos : unc, f3);
+  r->vel = (float*)dupmem(vel, f3);
+  if (!vel && r->vel) memset(r->vel, 0, f3);
+  r->frc = (float*)calloc(3 * (size_t)n + 1, sizeof(float));
+  r->incr = (float*)calloc(3 * (size_t)n + 1, sizeof(float));
+  r->type = type ? (int*)dupmem(type, sizeof(int) * (size_t)n) : NULL;
+  r->bi = (int*)dupmem(bi, sizeof(int) * (size_t)nbnd);
+  r->bj = (int*)dupmem(bj, sizeof(int) * (size_t)nbnd);
+  r->br0 = (float*)dupmem(br0, sizeof(float) * (size_t)nbnd);
+  r->ai = (int*)dupmem(ai, sizeof(int) * (size_t)nang);
+  r->ak = (int*)dupmem(ak, sizeof(int) * (size_t)nang);
+  r->ni = (int*)dupmem(ni, sizeof(int) * (size_t)nnat);
+  r->nj = (int*)dupmem(nj, sizeof(int) * (size_t)nnat);
+  r->nr0 = (float*)dupmem(nr0, sizeof(float) * (size_t)nnat);
+  r->neps = (float*)dupmem(neps, sizeof(float) * (size_t)nnat);
+  memcpy(r->params, params, sizeof(r->params));
+  memcpy(r->cut, cut, sizeof(r->cut));
   double cc[5];
   orc_langevin_consts(h, zeta, T, cc);
-  const float a1 = (float)cc[0], a2 = (float)cc[1], a3 = (float)cc[2], a4 = (float)cc[3];
-  const float var = (float)cc[4];
-  long long cap = (long long)n * 64 + 1024;
-  int* nl_att = (int*)malloc(sizeof(int) * (size_t)(nnat + 1));
-  int* pl_att = (int*)malloc(sizeof(int) * (size_t)(nnat + 1));
-  int* nli = (int*)malloc(sizeof(int) * (size_t)cap);
-  int* nlj = (int*)malloc(sizeof(int) * (size_t)cap);
-  int* pli = (int*)malloc(sizeof(int) * (size_t)cap);
-  int* plj = (int*)malloc(sizeof(int) * (size_t)cap);
-  float* frc = (float*)malloc(sizeof(float) * 3 * (size_t)n);
-  float* incr = (float*)malloc(sizeof(float) * 3 * (size_t)n);
-  if (!nl_att || !pl_att || !nli || !nlj || !pli || !plj || !frc || !incr) {
-    free(nl_att); free(pl_att); free(nli); free(nlj); free(pli); free(plj); free(frc); free(incr);
-    return -1;
+  r->a1 = (float)cc[0]; r->a2 = (float)cc[1]; r->a3 = (float)cc[2]; r->a4 = (float)cc[3];
+  r->var = (float)cc[4];
+  r->cap = (long long)n * 64 + 1024;
+  r->nl_att = (int*)malloc(sizeof(int) * (size_t)(nnat + 1));
+  r->pl_att = (int*)malloc(sizeof(int) * (size_t)(nnat + 1));
+  r->nli = (int*)malloc(sizeof(int) * (size_t)r->cap);
+  r->nlj = (int*)malloc(sizeof(int) * (size_t)r->cap);
+  r->pli = (int*)malloc(sizeof(int) * (size_t)r->cap);
+  r->plj = (int*)malloc(sizeof(int) * (size_t)r->cap);
+  r->key[0] = (uint32_t)seed; r->key[1] = (uint32_t)(seed >> 32);
+  r->traj = traj;
+  r->step = -1;  /* step 0 (initial lists and forces) not yet done */
+  if (!r->unc || !r->pos || !r->vel || !r->frc || !r->incr || !r->bi || !r->bj || !r->br0 ||
+      !r->ai || !r->ak || !r->ni || !r->nj || !r->nr0 || !r->neps || !r->nl_att || !r->pl_att ||
+      !r->nli || !r->nlj || !r->pli || !r->plj) {
+    orc_ref_destroy(r);
+    return NULL;
   }
-  int nnl_att = 0, nil_att = 0;
-  long long nnl_rep = 0, nil_rep = 0;
-  uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  return r;
+}
 
-  for (long long step = 0; step <= nsteps; ++step) {
-    /* step 0 is the initial force evaluation of sop.cu:142-186 */
-    if (step == 0 || (nnlup > 0 && step % nnlup == 0)) {
-      nnl_att = orc_filter_att(unc, nnat, NULL, ni, nj, nr0, cut[0], cut[1], params[P_BOXL], nl_att);
-      for (;;) {
-        long long need = orc_nl_rep(n, unc, type, nnat, ni, nj, cut[2], cut[3], params[P_BOXL],
-                                    cap, nli, nlj);
-        if (need <= cap) { nnl_rep = need; break; }
-        cap = need + need / 4;
-        int* t1 = (int*)realloc(nli, sizeof(int) * (size_t)cap);
-        int* t2 = (int*)realloc(nlj, sizeof(int) * (size_t)cap);
-        int* t3 = (int*)realloc(pli, sizeof(int) * (size_t)cap);
-        int* t4 = (int*)realloc(plj, sizeof(int) * (size_t)cap);
-        if (t1) nli = t1;
-        if (t2) nlj = t2;
-        if (t3) pli = t3;
-        if (t4) plj = t4;
-        if (!t1 || !t2 || !t3 || !t4) { nsteps = step - 1; goto done; }
+static int ref_lists(orc_ref* r, int nl, int pl) {
+  const double boxl = r->params[P_BOXL];
+  if (nl) {
+    r->nnl_att = orc_filter_att(r->unc, r->nnat, NULL, r->ni, r->nj, r->nr0, r->cut[0], r->cut[1],
+                                boxl, r->nl_att);
+    for (;;) {
+      long long need = orc_nl_rep(r->n, r->unc, r->type, r->nnat, r->ni, r->nj, r->cut[2],
+                                  r->cut[3], boxl, r->cap, r->nli, r->nlj);
+      if (need <= r->cap) { r->nnl_rep = need; break; }
+      long long cap = need + need / 4;
+      int* t[4];
+      int** slot[4] = {&r->nli, &r->nlj, &r->pli, &r->plj};
+      for (int q = 0; q < 4; ++q) {
+        t[q] = (int*)realloc(*slot[q], sizeof(int) * (size_t)cap);
+        if (!t[q]) return -1;
+        *slot[q] = t[q];
       }
+      r->cap = cap;
     }
-    if (step == 0 || (nplup > 0 && step % nplup == 0) || (nnlup > 0 && step % nnlup == 0)) {
-      nil_att = orc_filter_att(unc, nnl_att, nl_att, ni, nj, nr0, cut[4], cut[5], params[P_BOXL], pl_att);
-      nil_rep = orc_filter_rep(unc, type, nnl_rep, nli, nlj, cut[6], cut[7], params[P_BOXL], pli, plj);
-    }
-    if (step > 0) {
-      for (int q = 0; q < 3 * n; ++q) {
-        incr[q] = a1 * vel[q] + a2 * frc[q];
-        float p = pos[q] + incr[q];
-        pos[q] = p - boxl * rintf(p / boxl);
-        unc[q] += incr[q];
-      }
-    }
-    /* force_eval: clear, noise, FENE, soft sphere, att, rep (energy.cu:81-150) */
-    memset(frc, 0, sizeof(float) * 3 * (size_t)n);
-    for (int i = 0; i < n; ++i) {
-      uint32_t ctr[4] = {(uint32_t)i, (uint32_t)step, (uint32_t)((unsigned long long)step >> 32), traj};
-      uint32_t r[4];
-      orc_philox4x32_10(ctr, key, r);
-      float m0 = sqrtf(-2.0f * logf(u01f(r[0])));
-      float m1 = sqrtf(-2.0f * logf(u01f(r[2])));
-      float t0 = 6.2831853f * u01f(r[1]), t1 = 6.2831853f * u01f(r[3]);
-      frc[3 * i + 0] += var * m0 * cosf(t0);
-      frc[3 * i + 1] += var * m0 * sinf(t0);
-      frc[3 * i + 2] += var * m1 * cosf(t1);
-    }
-    for (int b = 0; b < nbnd; ++b) {
-      int i = bi[b], j = bj[b];
-      float dx = unc[3 * j] - unc[3 * i], dy = unc[3 * j + 1] - unc[3 * i + 1],
-            dz = unc[3 * j + 2] - unc[3 * i + 2];
-      dx -= boxl * rintf(dx / boxl); dy -= boxl * rintf(dy / boxl); dz -= boxl * rintf(dz / boxl);
-      float d = sqrtf(dx * dx + dy * dy + dz * dz);
-      float dev = d - br0[b];
-      float tmp = -k_bnd * dev / d / (1.0f - dev * dev / R0sq);
-      frc[3 * i] -= tmp * dx; frc[3 * i + 1] -= tmp * dy; frc[3 * i + 2] -= tmp * dz;
-      frc[3 * j] += tmp * dx; frc[3 * j + 1] += tmp * dy; frc[3 * j + 2] += tmp * dz;
-    }
-    for (int t = 0; t < nang; ++t) {
-      int i = ai[t], j = ak[t];
-      float dx = unc[3 * j] - unc[3 * i], dy = unc[3 * j + 1] - unc[3 * i + 1],
-            dz = unc[3 * j + 2] - unc[3 * i + 2];
-      dx -= boxl * rintf(dx / boxl); dy -= boxl * rintf(dy / boxl); dz -= boxl * rintf(dz / boxl);
-      float d = sqrtf(dx * dx + dy * dy + dz * dz);
-      float co1 = f_ang / powf(d, 8.0f);
-      frc[3 * i] -= co1 * dx; frc[3 * i + 1] -= co1 * dy; frc[3 * i + 2] -= co1 * dz;
-      frc[3 * j] += co1 * dx; frc[3 * j + 1] += co1 * dy; frc[3 * j + 2] += co1 * dz;
-    }
-    for (int p = 0; p < nil_att; ++p) {
-      int c = pl_att[p], i = ni[c], j = nj[c];
-      float dx = unc[3 * j] - unc[3 * i], dy = unc[3 * j + 1] - unc[3 * i + 1],
-            dz = unc[3 * j + 2] - unc[3 * i + 2];
-      dx -= boxl * rintf(dx / boxl); dy -= boxl * rintf(dy / boxl); dz -= boxl * rintf(dz / boxl);
-      float d2 = dx * dx + dy * dy + dz * dz;
-      float r02 = nr0[c] * nr0[c];
-      if (d2 > 1.0e-7f * r02) {
-        float d6 = d2 * d2 * d2, d12 = d6 * d6;
-        float r06 = r02 * r02 * r02, r012 = r06 * r06;
-        float co1 = -12.0f * neps[c] / d2 * ((r012 / d12) - (r06 / d6));
-        frc[3 * i] += co1 * dx; frc[3 * i + 1] += co1 * dy; frc[3 * i + 2] += co1 * dz;
-        frc[3 * j] -= co1 * dx; frc[3 * j + 1] -= co1 * dy; frc[3 * j + 2] -= co1 * dz;
-      }
-    }
-    for (long long p = 0; p < nil_rep; ++p) {
-      int i = pli[p], j = plj[p];
-      float dx = unc[3 * j] - unc[3 * i], dy = unc[3 * j + 1] - unc[3 * i + 1],
-            dz = unc[3 * j + 2] - unc[3 * i + 2];
-      dx -= boxl * rintf(dx / boxl); dy -= boxl * rintf(dy / boxl); dz -= boxl * rintf(dz / boxl);
-      float sg = kSigmaRepF[tp(type, i)][tp(type, j)];
-      float s2 = sg * sg, s6 = s2 * s2 * s2, s12 = s6 * s6;
-      float d2 = dx * dx + dy * dy + dz * dz;
-      if (d2 > sg * 1.0e-7f) {
-        float d6 = d2 * d2 * d2, d12 = d6 * d6;
-        float co1 = -6.0f * eps_rep / d2 * (2.0f * s12 / d12 + s6 / d6);
-        frc[3 * i] += co1 * dx; frc[3 * i + 1] += co1 * dy; frc[3 * i + 2] += co1 * dz;
-        frc[3 * j] -= co1 * dx; frc[3 * j + 1] -= co1 * dy; frc[3 * j + 2] -= co1 * dz;
-      }
-    }
-    if (step > 0)
-      for (int q = 0; q < 3 * n; ++q) vel[q] = a3 * incr[q] + a4 * frc[q];
   }
-done:
-  free(nl_att); free(pl_att); free(nli); free(nlj); free(pli); free(plj); free(frc); free(incr);
+  if (pl) {
+    r->nil_att = orc_filter_att(r->unc, r->nnl_att, r->nl_att, r->ni, r->nj, r->nr0, r->cut[4],
+                                r->cut[5], boxl, r->pl_att);
+    r->nil_rep = orc_filter_rep(r->unc, r->type, r->nnl_rep, r->nli, r->nlj, r->cut[6], r->cut[7],
+                                boxl, r->pli, r->plj);
+  }
+  return 0;
+}
+
+/* force_eval: clear, noise, FENE, soft sphere, att, rep (energy.cu:81-150) */
+static void ref_forces(orc_ref* r) {
+  const int n = r->n;
+  const float boxl = (float)r->params[P_BOXL];
+  const float k_bnd = (float)r->params[P_KBND];
+  const float R0sq = (float)(r->params[P_R0] * r->params[P_R0]);
+  const float f_ang = (float)(6.0 * r->params[P_EPS_SS] * pow(r->params[P_SIG_SS], 6.0));
+  const float eps_rep = (float)r->params[P_EPS_REP];
+  float* unc = r->unc;
+  float* frc = r->frc;
+  memset(frc, 0, sizeof(float) * 3 * (size_t)n);
+  for (int i = 0; i < n; ++i) {
+    uint32_t ctr[4] = {(uint32_t)i, (uint32_t)r->step, (uint32_t)((unsigned long long)r->step >> 32),
+                       r->traj};
+    uint32_t q[4];
+    orc_philox4x32_10(ctr, r->key, q);
+    float m0 = sqrtf(-2.0f * logf(u01f(q[0])));
+    float m1 = sqrtf(-2.0f * logf(u01f(q[2])));
+    float t0 = 6.2831853f * u01f(q[1]), t1 = 6.2831853f * u01f(q[3]);
+    frc[3 * i + 0] += r->var * m0 * cosf(t0);
+    frc[3 * i + 1] += r->var * m0 * sinf(t0);
+    frc[3 * i + 2] += r->var * m1 * cosf(t1);
+  }
+  for (int b = 0; b < r->nbnd; ++b) {
+    int i = r->bi[b], j = r->bj[b];
+    float dx = unc[3 * j] - unc[3 * i], dy = unc[3 * j + 1] - unc[3 * i + 1],
+          dz = unc[3 * j + 2] - unc[3 * i + 2];
+    dx -= boxl * rintf(dx / boxl); dy -= boxl * rintf(dy / boxl); dz -= boxl * rintf(dz / boxl);
+    float d = sqrtf(dx * dx + dy * dy + dz * dz);
+    float dev = d - r->br0[b];
+    float tmp = -k_bnd * dev / d / (1.0f - dev * dev / R0sq);
+    frc[3 * i] -= tmp * dx; frc[3 * i + 1] -= tmp * dy; frc[3 * i + 2] -= tmp * dz;
+    frc[3 * j] += tmp * dx; frc[3 * j + 1] += tmp * dy; frc[3 * j + 2] += tmp * dz;
+  }
+  for (int t = 0; t < r->nang; ++t) {
+    int i = r->ai[t], j = r->ak[t];
+    float dx = unc[3 * j] - unc[3 * i], dy = unc[3 * j + 1] - unc[3 * i + 1],
+          dz = unc[3 * j + 2] - unc[3 * i + 2];
+    dx -= boxl * rintf(dx / boxl); dy -= boxl * rintf(dy / boxl); dz -= boxl * rintf(dz / boxl);
+    float d = sqrtf(dx * dx + dy * dy + dz * dz);
+    float co1 = f_ang / powf(d, 8.0f);
+    frc[3 * i] -= co1 * dx; frc[3 * i + 1] -= co1 * dy; frc[3 * i + 2] -= co1 * dz;
+    frc[3 * j] += co1 * dx; frc[3 * j + 1] += co1 * dy; frc[3 * j + 2] += co1 * dz;
+  }
+  for (int p = 0; p < r->nil_att; ++p) {
+    int c = r->pl_att[p], i = r->ni[c], j = r->nj[c];
+    float dx = unc[3 * j] - unc[3 * i], dy = unc[3 * j + 1] - unc[3 * i + 1],
+          dz = unc[3 * j + 2] - unc[3 * i + 2];
+    dx -= boxl * rintf(dx / boxl); dy -= boxl * rintf(dy / boxl); dz -= boxl * rintf(dz / boxl);
+    float d2 = dx * dx + dy * dy + dz * dz;
+    float r02 = r->nr0[c] * r->nr0[c];
+    if (d2 > 1.0e-7f * r02) {
+      float d6 = d2 * d2 * d2, d12 = d6 * d6;
+      float r06 = r02 * r02 * r02, r012 = r06 * r06;
+      float co1 = -12.0f * r->neps[c] / d2 * ((r012 / d12) - (r06 / d6));
+      frc[3 * i] += co1 * dx; frc[3 * i + 1] += co1 * dy; frc[3 * i + 2] += co1 * dz;
+      frc[3 * j] -= co1 * dx; frc[3 * j + 1] -= co1 * dy; frc[3 * j + 2] -= co1 * dz;
+    }
+  }
+  for (long long p = 0; p < r->nil_rep; ++p) {
+    int i = r->pli[p], j = r->plj[p];
+    float dx = unc[3 * j] - unc[3 * i], dy = unc[3 * j + 1] - unc[3 * i + 1],
+          dz = unc[3 * j + 2] - unc[3 * i + 2];
+    dx -= boxl * rintf(dx / boxl); dy -= boxl * rintf(dy / boxl); dz -= boxl * rintf(dz / boxl);
+    float sg = kSigmaRepF[tp(r->type, i)][tp(r->type, j)];
+    float s2 = sg * sg, s6 = s2 * s2 * s2, s12 = s6 * s6;
+    float d2 = dx * dx + dy * dy + dz * dz;
+    if (d2 > sg * 1.0e-7f) {
+      float d6 = d2 * d2 * d2, d12 = d6 * d6;
+      float co1 = -6.0f * eps_rep / d2 * (2.0f * s12 / d12 + s6 / d6);
+      frc[3 * i] += co1 * dx; frc[3 * i + 1] += co1 * dy; frc[3 * i + 2] += co1 * dz;
+      frc[3 * j] -= co1 * dx; frc[3 * j + 1] -= co1 * dy; frc[3 * j + 2] -= co1 * dz;
+    }
+  }
+}
+
+/* Advances nsteps steps (the first call also runs step 0, the initial lists
+ * and forces of sop.cu:142-186).  Returns the steps run, or -1 on failure. */
+long long orc_ref_advance(orc_ref* r, long long nsteps) {
+  if (!r) return -1;
+  const float boxl = (float)r->params[P_BOXL];
+  const int n3 = 3 * r->n;
+  if (r->step < 0) {
+    r->step = 0;
+    if (ref_lists(r, 1, 1)) return -1;
+    ref_forces(r);
+  }
+  for (long long k = 0; k < nsteps; ++k) {
+    const long long st = ++r->step;
+    const int nl = r->nnlup > 0 && st % r->nnlup == 0;
+    const int pl = nl || r->nplup <= 1 || st % r->nplup == 0;
+    if ((nl || pl) && ref_lists(r, nl, pl)) return -1;
+    for (int q = 0; q < n3; ++q) {
+      r->incr[q] = r->a1 * r->vel[q] + r->a2 * r->frc[q];
+      float p = r->pos[q] + r->incr[q];
+      r->pos[q] = p - boxl * rintf(p / boxl);
+      r->unc[q] += r->incr[q];
+    }
+    ref_forces(r);
+    for (int q = 0; q < n3; ++q) r->vel[q] = r->a3 * r->incr[q] + r->a4 * r->frc[q];
+  }
   return nsteps;
+}
+
+void orc_ref_state(const orc_ref* r, float* unc, float* pos, float* vel) {
+  size_t f3 = sizeof(float) * 3 * (size_t)r->n;
+  if (unc) memcpy(unc, r->unc, f3);
+  if (pos) memcpy(pos, r->pos, f3);
+  if (vel) memcpy(vel, r->vel, f3);
 }

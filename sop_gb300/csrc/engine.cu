@@ -31,9 +31,9 @@ void launch_pl_rebuild(const DevSys& s, int koff, cudaStream_t st);
 void launch_scan(const int* in, long long n, int* out, int* block_sums, cudaStream_t st);
 long long scan_block_sums_needed(long long n);
 // kernels_step.cu
-void launch_step(const DevSys& s, int G, const int2* tiles, int ntiles, int koff, bool step,
-                 cudaStream_t st);
+void launch_step(const DevSys& s, int G, int koff, bool step, cudaStream_t st);
 void launch_advance(const DevSys& s, int steps, cudaStream_t st);
+void launch_gather_current(const DevSys& s, float4* out, cudaStream_t st);
 void launch_energy(const DevSys& s, int mol_start, int mol_n, int m, double* part, double* out,
                    double k_bnd_R0sq_half, cudaStream_t st);
 void launch_observables(const DevSys& s, int mol_start, int mol_n, int m, int nnat,
@@ -99,11 +99,10 @@ struct SopCtx {
   long long bytes = 0;
   NLScratch w{};
   int G = 8;
-  int2* tiles = nullptr;
-  int ntiles = 0;
   double* e_part = nullptr;   // energy / observable partials
   double* e_out = nullptr;    // 8 doubles
   double* h_out = nullptr;    // pinned copy of e_out
+  float4* stage = nullptr;    // gather buffer of sop_download_all
   long long host_step = 0;    // common step of plain / batched contexts
   long long target_step = 0;  // step every molecule should reach after the queued work
   std::map<std::string, Graph> graphs;
@@ -216,7 +215,7 @@ int nl_rebuild_checked(SopCtx* ctx, int koff) {
 }
 
 void force_eval_async(SopCtx* ctx) {
-  launch_step(ctx->s, ctx->G, ctx->tiles, ctx->ntiles, 0, false, ctx->stream);
+  launch_step(ctx->s, ctx->G, 0, false, ctx->stream);
 }
 
 // Which rebuilds precede step n (1-based): bit 0 neighbour list, bit 1 pair list.
@@ -234,7 +233,7 @@ void enqueue_block(SopCtx* ctx, long long s0, int count) {
     int r = rebuilds_before(ctx->P, s0 + 1 + k);
     if (r & 1) launch_nl_rebuild(ctx->s, ctx->w, k, ctx->stream);
     if (r & 2) launch_pl_rebuild(ctx->s, k, ctx->stream);
-    launch_step(ctx->s, ctx->G, ctx->tiles, ctx->ntiles, k, true, ctx->stream);
+    launch_step(ctx->s, ctx->G, k, true, ctx->stream);
   }
   launch_advance(ctx->s, count, ctx->stream);
 }
@@ -320,18 +319,6 @@ int sync_checked(SopCtx* ctx) {
   return ctx->fail(SOP_ERR_CAPACITY, "neighbour list kept overflowing");
 }
 
-int build_tiles(SopCtx* ctx) {
-  const int bpb = 256 / ctx->G;
-  std::vector<int2> t;
-  for (int b = 0; b < ctx->s.nbead; b += bpb) t.push_back(make_int2(b, std::min(bpb, ctx->s.nbead - b)));
-  if (ctx->tiles) ctx->dfree(ctx->tiles);
-  ctx->tiles = ctx->dalloc<int2>(t.size());
-  if (!ctx->tiles) return ctx->fail(SOP_ERR_ALLOC, "tile allocation failed");
-  ctx->ntiles = (int)t.size();
-  CK(cudaMemcpy(ctx->tiles, t.data(), sizeof(int2) * t.size(), cudaMemcpyHostToDevice));
-  return SOP_OK;
-}
-
 MolConst make_const(const sop_params& P, const HostMol& hm) {
   MolConst c{};
   c.start = hm.start;
@@ -376,6 +363,7 @@ int commit(SopCtx* ctx) {
     for (int b = 0; b < 3; ++b) {
       float sg = kSigmaRep[a][b];
       s.sig2[a][b] = sg * sg;
+      s.rep_tol[a][b] = sg * 1.0e-7f;
       s.rc2_nl_rep[a][b] = rcut2_of(P.nl_rep_fac, P.nl_rep_abs, sg);
       s.rc2_pl_rep[a][b] = rcut2_of(P.pl_rep_fac, P.pl_rep_abs, sg);
       if (a > 0 && b > 0) rcmax = std::max(rcmax, rcut_of(P.nl_rep_fac, P.nl_rep_abs, sg));
@@ -546,10 +534,8 @@ int commit(SopCtx* ctx) {
   CK(cudaMemsetAsync(s.nl_maxrow, 0, sizeof(int), st));
 
   ctx->G = lanes_for(ctx);
-  int rc = build_tiles(ctx);
-  if (rc) return rc;
   // set-up of underdamped_ctrl: lists from x_0, then f_0 and the look-ahead
-  rc = nl_rebuild_checked(ctx, 0);
+  int rc = nl_rebuild_checked(ctx, 0);
   if (rc) return rc;
   launch_pl_rebuild(s, 0, st);
   force_eval_async(ctx);
@@ -750,6 +736,35 @@ int sop_step(void* p, long long nsteps) {
   return sync_checked(ctx);
 }
 
+int sop_step_async(void* p, long long nsteps) {
+  if (!p || nsteps < 0) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (!ctx->committed) return ctx->fail(SOP_ERR_ARG, "context not committed");
+  return step_async(ctx, nsteps);
+}
+
+int sop_sync(void* p) {
+  if (!p) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (!ctx->committed) return ctx->fail(SOP_ERR_ARG, "context not committed");
+  return sync_checked(ctx);
+}
+
+int sop_launch_stage(void* p, int stage, int koff) {
+  if (!p) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (!ctx->committed) return ctx->fail(SOP_ERR_ARG, "context not committed");
+  switch (stage) {
+    case 0: launch_step(ctx->s, ctx->G, koff, true, ctx->stream); break;
+    case 1: launch_pl_rebuild(ctx->s, koff, ctx->stream); break;
+    case 2: launch_nl_rebuild(ctx->s, ctx->w, koff, ctx->stream); break;
+    case 3: launch_advance(ctx->s, koff, ctx->stream); break;
+    default: return ctx->fail(SOP_ERR_ARG, "unknown stage");
+  }
+  CK(cudaGetLastError());
+  return SOP_OK;
+}
+
 int sop_update_neighbor_list(void* p, long long* nnl_att, long long* nnl_rep) {
   if (!p) return SOP_ERR_ARG;
   SopCtx* ctx = C(p);
@@ -914,6 +929,41 @@ int sop_download_list(void* p, int mol, int which, long long cap, int* i_out, in
       for (int t = 0; t < cnt[i]; ++t) emit(i, jj[(size_t)i * stride + t] - o, 0.f);
   }
   if (count) *count = k;
+  return SOP_OK;
+}
+
+int sop_list_sizes(void* p, long long* out) {
+  if (!p || !out) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (!ctx->committed) return ctx->fail(SOP_ERR_ARG, "context not committed");
+  int rc = sync_checked(ctx);
+  if (rc) return rc;
+  const int* src[4] = {ctx->s.nl_att_cnt, ctx->s.nl_cnt, ctx->s.pl_att_cnt, ctx->s.pl_cnt};
+  std::vector<int> h(ctx->s.nbead);
+  for (int t = 0; t < 4; ++t) {
+    CK(cudaMemcpy(h.data(), src[t], sizeof(int) * h.size(), cudaMemcpyDeviceToHost));
+    long long sum = 0;
+    for (int v : h) sum += v;
+    out[t] = sum / 2;  // full rows hold each pair twice
+  }
+  return SOP_OK;
+}
+
+int sop_download_all(void* p, float* unc_pos) {
+  if (!p || !unc_pos) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (!ctx->committed) return ctx->fail(SOP_ERR_ARG, "context not committed");
+  int rc = sync_checked(ctx);
+  if (rc) return rc;
+  if (!ctx->stage) {
+    ctx->stage = ctx->dalloc<float4>(ctx->s.nbead);
+    if (!ctx->stage) return ctx->fail(SOP_ERR_ALLOC, "staging buffer allocation failed");
+  }
+  launch_gather_current(ctx->s, ctx->stage, ctx->stream);
+  CK(cudaGetLastError());
+  rc = copy3(ctx, unc_pos, ctx->stage, ctx->s.nbead);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
   return SOP_OK;
 }
 

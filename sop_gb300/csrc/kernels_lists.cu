@@ -4,8 +4,8 @@
 //
 // Neighbour list (every nnlup steps):
 //   1. per-molecule bounding box of the coordinates             k_bbox
-//   2. per-molecule cell grid (cell edge rc/S, S=1..4 chosen so a cell holds
-//      ~1.5 beads; molecules whose extent + rc reaches boxl, where the minimum
+//   2. per-molecule cell grid (cell edge rc/S, S=1..3 chosen so a cell holds
+//      ~4 beads; molecules whose extent + rc reaches boxl, where the minimum
 //      image matters, fall back to index-chunked cells that scan all pairs)
 //                                                                k_grid, k_grid_base
 //   3. counting sort of beads into cells (own scan), cells sorted by bead id
@@ -179,8 +179,8 @@ __global__ void k_grid(DevSys s, int* __restrict__ ncell) {
   } else {
     float vol = fmaxf((ext[0] + 1.0f) * (ext[1] + 1.0f) * (ext[2] + 1.0f), 1.0f);
     float rho = (float)n / vol;
-    int S = (int)floorf(rc * cbrtf(rho * (1.0f / 1.5f)));
-    S = S < 1 ? 1 : (S > 4 ? 4 : S);
+    int S = (int)floorf(rc * cbrtf(rho * 0.25f));
+    S = S < 1 ? 1 : (S > 3 ? 3 : S);
     float cs = rc * 1.0001f / (float)S + 1.0e-4f;
     long long cap = n * 2 > 64 ? (long long)n * 2 : 64;
     for (int iter = 0; iter < 8; ++iter) {
@@ -265,9 +265,9 @@ __global__ void k_assign(DevSys s, int koff) {
   for (int e = 0; e < row.y; ++e) {
     int idx = row.x + e;
     float4 xj = X[s.nat_j[idx]];
-    float dx = min_image(__fsub_rn(xj.x, xi.x), s.boxl);
-    float dy = min_image(__fsub_rn(xj.y, xi.y), s.boxl);
-    float dz = min_image(__fsub_rn(xj.z, xi.z), s.boxl);
+    float dx = __fsub_rn(xj.x, xi.x), dy = __fsub_rn(xj.y, xi.y),
+          dz = __fsub_rn(xj.z, xi.z);
+    min_image3(dx, dy, dz, s.boxl);
     if (d2_exact(dx, dy, dz) < s.nat_rc2[idx].x) s.nl_att_e[row.x + k++] = idx;
   }
   s.nl_att_cnt[i] = k;
@@ -377,9 +377,9 @@ __global__ void __launch_bounds__(256) k_nl(DevSys s) {
           const int wj = __float_as_int(xj.w);
           j = wj >> 2;
           if (abs(j - i) > 2) {
-            const float dx = min_image(__fsub_rn(xj.x, xi.x), boxl);
-            const float dy2 = min_image(__fsub_rn(xj.y, xi.y), boxl);
-            const float dz2 = min_image(__fsub_rn(xj.z, xi.z), boxl);
+            float dx = __fsub_rn(xj.x, xi.x), dy2 = __fsub_rn(xj.y, xi.y),
+                  dz2 = __fsub_rn(xj.z, xi.z);
+            min_image3(dx, dy2, dz2, boxl);
             pass = d2_exact(dx, dy2, dz2) < pick_type_pair(r11, r12, r22, ti, wj & 3);
             if (pass) {
               bool native = false;
@@ -416,9 +416,11 @@ __global__ void __launch_bounds__(256) k_nl(DevSys s) {
 // the bead's attractive neighbour list.
 __global__ void __launch_bounds__(256) k_pl(DevSys s, int koff) {
   const int lane = threadIdx.x & 31;
-  const int i = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  if (i >= s.nbead) return;
+  // beads in cell order: the warps of a block gather from the same region
+  const int kk = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (kk >= s.cell_start[s.cell_cap]) return;
   if (*s.flags & FLAG_NL_OVERFLOW) return;
+  const int i = s.sorted[kk];
   const int m = s.mol_of[i];
   if (!mol_listed(s, m)) {
     if (lane == 0) { s.pl_cnt[i] = 0; s.pl_att_cnt[i] = 0; }
@@ -447,9 +449,9 @@ __global__ void __launch_bounds__(256) k_pl(DevSys s, int koff) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const float4 xj = X[e + q < cnt ? jq[q] : i];
-      const float dx = min_image(__fsub_rn(xj.x, xi.x), boxl);
-      const float dy = min_image(__fsub_rn(xj.y, xi.y), boxl);
-      const float dz = min_image(__fsub_rn(xj.z, xi.z), boxl);
+      float dx = __fsub_rn(xj.x, xi.x), dy = __fsub_rn(xj.y, xi.y),
+            dz = __fsub_rn(xj.z, xi.z);
+      min_image3(dx, dy, dz, boxl);
       pq[q] = (e + q < cnt) && d2_exact(dx, dy, dz) < pick_type_pair(r11, r12, r22, ti, type_of(xj));
       c += pq[q] ? 1 : 0;
     }
@@ -475,9 +477,9 @@ __global__ void __launch_bounds__(256) k_pl(DevSys s, int koff) {
       idx = s.nl_att_e[row.x + e];
       j = s.nat_j[idx];
       float4 xj = X[j];
-      float dx = min_image(__fsub_rn(xj.x, xi.x), boxl);
-      float dy = min_image(__fsub_rn(xj.y, xi.y), boxl);
-      float dz = min_image(__fsub_rn(xj.z, xi.z), boxl);
+      float dx = __fsub_rn(xj.x, xi.x), dy = __fsub_rn(xj.y, xi.y),
+            dz = __fsub_rn(xj.z, xi.z);
+      min_image3(dx, dy, dz, boxl);
       pass = d2_exact(dx, dy, dz) < s.nat_rc2[idx].y;
     }
     const unsigned mask = __ballot_sync(0xffffffffu, pass);

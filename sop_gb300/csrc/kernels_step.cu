@@ -31,154 +31,175 @@ __device__ __forceinline__ float group_sum(float v, unsigned gmask) {
 // STEP = false: force evaluation only at step mol_step + koff (velocities kept),
 // followed by the look-ahead; used after set-up and state uploads.
 template <int G, bool STEP>
-__global__ void __launch_bounds__(256) k_step(DevSys s, const int2* __restrict__ tiles, int koff) {
-  const int2 tile = tiles[blockIdx.x];
+__global__ void __launch_bounds__(256) k_step(DevSys s, int koff) {
+  constexpr int BPB = 256 / G;          // beads per block
+  __shared__ float4 fsum[BPB];          // conservative force sums; w = FENE range flag
+  __shared__ int bead[BPB];             // bead of each slot, -1: nothing to do
   const int slot = threadIdx.x / G;
   const int lane = threadIdx.x % G;
-  if (slot >= tile.y) return;
-  if (*s.flags & FLAG_NL_OVERFLOW) return;
-  const int i = tile.x + slot;
-  const int m = s.mol_of[i];
-  if (m < 0) return;
-  const MolConst mc = s.mol[m];
-  const long long n = s.mol_step[m] + (STEP ? 1 : 0) + koff;
-  if (!mc.active || s.mol_status[m] != 0 || (STEP && mc.nsteps >= 0 && n > mc.nsteps)) return;
-  const unsigned gmask = (G == 32) ? 0xffffffffu
-                                   : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
-  const int cur = (int)(n & 1);
-  const float4* __restrict__ X = s.x[cur];
-  const float4 xi = X[i];
-  const float boxl = s.boxl;
+  const int k = blockIdx.x * BPB + slot; // position in cell order
+  const int nbinned = s.cell_start[s.cell_cap];
+  int i = -1;
+  long long n = 0;
+  if (k < nbinned && !(*s.flags & FLAG_NL_OVERFLOW)) {
+    const int b = s.sorted[k];
+    const int m = s.mol_of[b];
+    const MolConst& mc = s.mol[m];
+    n = s.mol_step[m] + (STEP ? 1 : 0) + koff;
+    if (mc.active && s.mol_status[m] == 0 && !(STEP && mc.nsteps >= 0 && n > mc.nsteps)) i = b;
+  }
   float fx = 0.f, fy = 0.f, fz = 0.f;
   bool fene_bad = false;
+  if (i >= 0) {  // uniform over the lane group
+    const unsigned gmask = (G == 32) ? 0xffffffffu
+                                     : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+    const float4* __restrict__ X = s.x[(int)(n & 1)];
+    const float4 xi = X[i];
+    const float boxl = s.boxl;
+    // Row descriptors first, as independent loads.
+    const int2 br = s.bond_row[i];
+    const int2 ar = s.ang_row[i];
+    const int abase = s.nat_row[i].x;
+    const int acnt = s.pl_att_cnt[i];
+    const long long rbase = (long long)i * s.nl_stride;
+    const int rcnt = s.pl_cnt[i];
 
-  // Row descriptors first, as independent loads.
-  const int2 br = s.bond_row[i];
-  const int2 ar = s.ang_row[i];
-  const int abase = s.nat_row[i].x;
-  const int acnt = s.pl_att_cnt[i];
-  const long long rbase = (long long)i * s.nl_stride;
-  const int rcnt = s.pl_cnt[i];
-
-  // Bonded, angle and native terms share one index space [bonds | angles |
-  // natives]; a bead has a handful of them, usually one pass of the group.
-  const int nba = br.y + ar.y;
-  const int nsmall = nba + acnt;
-  for (int e = lane; e < nsmall; e += G) {
-    int j;
-    float r0 = 0.f, eps = 0.f;
-    if (e < br.y) {
-      j = s.bond_j[br.x + e];
-      r0 = s.bond_r0[br.x + e];
-    } else if (e < nba) {
-      j = s.ang_j[ar.x + e - br.y];
-    } else {
-      const float4 q = s.pl_att[abase + e - nba];
-      j = __float_as_int(q.x);
-      r0 = q.y;
-      eps = q.z;
+    // Bonded, angle and native terms share one index space [bonds | angles |
+    // natives]; a bead has a handful of them, usually one pass of the group.
+    const int nba = br.y + ar.y;
+    const int nsmall = nba + acnt;
+    for (int e = lane; e < nsmall; e += G) {
+      int j;
+      float r0 = 0.f, eps = 0.f;
+      if (e < br.y) {
+        j = s.bond_j[br.x + e];
+        r0 = s.bond_r0[br.x + e];
+      } else if (e < nba) {
+        j = s.ang_j[ar.x + e - br.y];
+      } else {
+        const float4 q = s.pl_att[abase + e - nba];
+        j = __float_as_int(q.x);
+        r0 = q.y;
+        eps = q.z;
+      }
+      const float4 xj = X[j];
+      float lx, ly, lz;
+      float dx = diff_exact(xj.x, xi.x, lx), dy = diff_exact(xj.y, xi.y, ly),
+            dz = diff_exact(xj.z, xi.z, lz);
+      min_image3(dx, dy, dz, boxl);
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      float c;
+      if (e < br.y) {
+        // FENE: force on i = +k dev / (r (1 - dev^2/R0^2)) * d  (energy.cu:252-271)
+        const float r = sqrtf(d2);
+        const float dev = d2_minus_r02(dx, dy, dz, lx, ly, lz, r0) / (r + r0);
+        const float w = 1.0f - dev * dev / s.R0sq;
+        fene_bad |= !(fabsf(dev) < s.R0);
+        c = s.k_bnd * dev / (r * w);
+      } else if (e < nba) {
+        // i,i+2 soft sphere: force on i = -6 eps sigma^6 / d^8 * d  (energy.cu:335-360)
+        const float inv = __fdividef(1.0f, d2);
+        const float inv2 = inv * inv;
+        c = -s.f_ss * inv2 * inv2;
+      } else {
+        // native LJ 12-6 (energy.cu:468-507): co1 = -12 eps / d^2 (s^6 - s^3),
+        // s = r0^2 / d^2, as -12 eps / d^2 s^3 (s - 1)(s^2 + s + 1) with
+        // s - 1 = -(d^2 - r0^2) / d^2; pairs with d^2 <= 1e-7 r0^2 are skipped.
+        const float r02 = r0 * r0;
+        const float inv = __fdividef(1.0f, d2);
+        const float sr = r02 * inv;
+        const float sm1 = -d2_minus_r02(dx, dy, dz, lx, ly, lz, r0) * inv;
+        const float s3 = sr * sr * sr;
+        c = (d2 > 1.0e-7f * r02) ? -12.0f * eps * inv * s3 * sm1 * (sr * sr + sr + 1.0f) : 0.0f;
+      }
+      fx += c * dx; fy += c * dy; fz += c * dz;
     }
-    const float4 xj = X[j];
-    float lx, ly, lz;
-    const float dx = diff_exact(xj.x, xi.x, boxl, lx);
-    const float dy = diff_exact(xj.y, xi.y, boxl, ly);
-    const float dz = diff_exact(xj.z, xi.z, boxl, lz);
-    const float d2 = dx * dx + dy * dy + dz * dz;
-    float c;
-    if (e < br.y) {
-      // FENE: force on i = +k dev / (r (1 - dev^2/R0^2)) * d  (energy.cu:252-271)
-      const float r = sqrtf(d2);
-      const float dev = d2_minus_r02(dx, dy, dz, lx, ly, lz, r0) / (r + r0);
-      const float w = 1.0f - dev * dev / s.R0sq;
-      fene_bad |= !(fabsf(dev) < s.R0);
-      c = s.k_bnd * dev / (r * w);
-    } else if (e < nba) {
-      // i,i+2 soft sphere: force on i = -6 eps sigma^6 / d^8 * d  (energy.cu:335-360)
-      const float inv = 1.0f / d2;
-      const float inv2 = inv * inv;
-      c = -s.f_ss * inv2 * inv2;
-    } else {
-      // native LJ 12-6 (energy.cu:468-507): co1 = -12 eps / d^2 (s^6 - s^3),
-      // s = r0^2 / d^2, as -12 eps / d^2 s^3 (s - 1)(s^2 + s + 1) with
-      // s - 1 = -(d^2 - r0^2) / d^2; pairs with d^2 <= 1e-7 r0^2 are skipped.
-      const float r02 = r0 * r0;
-      const float inv = 1.0f / d2;
-      const float sr = r02 * inv;
-      const float sm1 = -d2_minus_r02(dx, dy, dz, lx, ly, lz, r0) * inv;
-      const float s3 = sr * sr * sr;
-      c = (d2 > 1.0e-7f * r02) ? -12.0f * eps * inv * s3 * sm1 * (sr * sr + sr + 1.0f) : 0.0f;
+
+    // Non-native repulsion (energy.cu:536-581): co1 = -6 eps / d^2 (2 (s/r)^12 +
+    // (s/r)^6) [rep6: -6 eps / d^2 (s/r)^6]; pairs with d^2 <= 1e-7 sigma are
+    // skipped.  Each lane takes 4 consecutive entries per iteration (one
+    // 16-byte load of the row, four independent gathers); entries past the row
+    // end read bead i itself, which the tolerance test drops.
+    const int ti = type_of(xi);
+    const float g11 = s.sig2[1][1], g12 = s.sig2[1][2], g22 = s.sig2[2][2];
+    const float t11 = s.rep_tol[1][1], t12 = s.rep_tol[1][2], t22 = s.rep_tol[2][2];
+    const float ce = -6.0f * s.eps_rep;
+    const float two = s.rep6 ? 0.0f : 2.0f;
+    auto rep = [&](const float4 xj) {
+      float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
+      min_image3(dx, dy, dz, boxl);
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      const int tj = type_of(xj);
+      const float sg2 = pick_type_pair(g11, g12, g22, ti, tj);
+      const float inv = __fdividef(1.0f, d2);
+      const float u = sg2 * inv;
+      const float u3 = u * u * u;
+      const float c = (d2 > pick_type_pair(t11, t12, t22, ti, tj)) ? ce * inv * u3 * (two * u3 + 1.0f) : 0.0f;
+      fx += c * dx; fy += c * dy; fz += c * dz;
+    };
+    const int4* prow = reinterpret_cast<const int4*>(s.pl_j + rbase);
+    for (int e = 4 * lane; e < rcnt; e += 4 * G) {
+      const int4 jv = prow[e >> 2];
+      const float4 x0 = X[jv.x];
+      const float4 x1 = X[e + 1 < rcnt ? jv.y : i];
+      const float4 x2 = X[e + 2 < rcnt ? jv.z : i];
+      const float4 x3 = X[e + 3 < rcnt ? jv.w : i];
+      rep(x0);
+      rep(x1);
+      rep(x2);
+      rep(x3);
     }
-    fx += c * dx; fy += c * dy; fz += c * dz;
+    fx = group_sum<G>(fx, gmask);
+    fy = group_sum<G>(fy, gmask);
+    fz = group_sum<G>(fz, gmask);
+    fene_bad = __any_sync(gmask, fene_bad);
   }
-
-  // Non-native repulsion (energy.cu:536-581): co1 = -6 eps / d^2 (2 (s/r)^12 +
-  // (s/r)^6) [rep6: -6 eps / d^2 (s/r)^6]; pairs with d^2 <= 1e-7 sigma are
-  // skipped.
-  const int ti = type_of(xi);
-  const float g11 = s.sig2[1][1], g12 = s.sig2[1][2], g22 = s.sig2[2][2];
-  const float ce = -6.0f * s.eps_rep;
-  const float two = s.rep6 ? 0.0f : 2.0f;
-  auto rep = [&](const float4 xj) {
-    const float dx = min_image(xj.x - xi.x, boxl);
-    const float dy = min_image(xj.y - xi.y, boxl);
-    const float dz = min_image(xj.z - xi.z, boxl);
-    const float d2 = dx * dx + dy * dy + dz * dz;
-    const float sg2 = pick_type_pair(g11, g12, g22, ti, type_of(xj));
-    const float inv = 1.0f / d2;
-    const float u = sg2 * inv;
-    const float u3 = u * u * u;
-    const float c = (d2 > sqrtf(sg2) * 1.0e-7f) ? ce * inv * u3 * (two * u3 + 1.0f) : 0.0f;
-    fx += c * dx; fy += c * dy; fz += c * dz;
-  };
-  // Each lane takes 4 consecutive entries per iteration (one 16-byte load of
-  // the row, four independent gathers); entries past the row end read bead i
-  // itself, which the d^2 > tol test drops.
-  const int4* prow = reinterpret_cast<const int4*>(s.pl_j + rbase);
-  for (int e = 4 * lane; e < rcnt; e += 4 * G) {
-    const int4 jv = prow[e >> 2];
-    const float4 x0 = X[jv.x];
-    const float4 x1 = X[e + 1 < rcnt ? jv.y : i];
-    const float4 x2 = X[e + 2 < rcnt ? jv.z : i];
-    const float4 x3 = X[e + 3 < rcnt ? jv.w : i];
-    rep(x0);
-    rep(x1);
-    rep(x2);
-    rep(x3);
+  if (lane == 0) {
+    fsum[slot] = make_float4(fx, fy, fz, fene_bad ? 1.0f : 0.0f);
+    bead[slot] = i;
   }
-  fx = group_sum<G>(fx, gmask);
-  fy = group_sum<G>(fy, gmask);
-  fz = group_sum<G>(fz, gmask);
-  const bool bad_any = __any_sync(gmask, fene_bad);
-  if (lane != 0) return;
+  __syncthreads();
+  if (threadIdx.x >= BPB) return;
 
+  // Per-bead epilogue, one thread per bead: noise, status, velocity and the
+  // look-ahead position update (sop.cu:421-462, energy.cu:588-604).
+  const int b = bead[threadIdx.x];
+  if (b < 0) return;
+  const int m = s.mol_of[b];
+  const MolConst mc = s.mol[m];
+  const long long nb = s.mol_step[m] + (STEP ? 1 : 0) + koff;
+  const int cur = (int)(nb & 1);
+  const float4 fs = fsum[threadIdx.x];
   float3 z;
   if (s.use_noise) {
-    const float4 q = s.noise[i];
+    const float4 q = s.noise[b];
     z = make_float3(q.x, q.y, q.z);
   } else {
-    z = noise3((unsigned)(i - mc.start), n, mc.traj, s.seed_lo, s.seed_hi);
+    z = noise3((unsigned)(b - mc.start), nb, mc.traj, s.seed_lo, s.seed_hi);
   }
-  fx += mc.sigma_f * z.x;
-  fy += mc.sigma_f * z.y;
-  fz += mc.sigma_f * z.z;
+  const float fxx = fs.x + mc.sigma_f * z.x;
+  const float fyy = fs.y + mc.sigma_f * z.y;
+  const float fzz = fs.z + mc.sigma_f * z.z;
   int st = 0;
-  if (bad_any) st |= SOP_MOL_FENE_RANGE;
-  if (!(isfinite(fx) && isfinite(fy) && isfinite(fz))) st |= SOP_MOL_NONFINITE;
+  if (fs.w != 0.0f) st |= SOP_MOL_FENE_RANGE;
+  if (!(isfinite(fxx) && isfinite(fyy) && isfinite(fzz))) st |= SOP_MOL_NONFINITE;
   if (st) atomicOr(s.mol_status + m, st);
-  s.f[i] = make_float4(fx, fy, fz, 0.f);
-  float4 vi = s.v[i];
-  float4 inc = s.incr[i];
+  s.f[b] = make_float4(fxx, fyy, fzz, 0.f);
+  float4 vi = s.v[b];
+  float4 inc = s.incr[b];
   if (STEP && !mc.t_zero) {
-    vi = make_float4(mc.a3 * inc.x + mc.a4 * fx, mc.a3 * inc.y + mc.a4 * fy,
-                     mc.a3 * inc.z + mc.a4 * fz, 0.f);
-    s.v[i] = vi;
+    vi = make_float4(mc.a3 * inc.x + mc.a4 * fxx, mc.a3 * inc.y + mc.a4 * fyy,
+                     mc.a3 * inc.z + mc.a4 * fzz, 0.f);
+    s.v[b] = vi;
   }
-  inc = make_float4(mc.a1 * vi.x + mc.a2 * fx, mc.a1 * vi.y + mc.a2 * fy,
-                    mc.a1 * vi.z + mc.a2 * fz, 0.f);
-  s.incr[i] = inc;
-  s.x[cur ^ 1][i] = make_float4(xi.x + inc.x, xi.y + inc.y, xi.z + inc.z, xi.w);
-  const float4 pi = s.p[cur][i];
-  s.p[cur ^ 1][i] = make_float4(min_image(pi.x + inc.x, boxl), min_image(pi.y + inc.y, boxl),
+  inc = make_float4(mc.a1 * vi.x + mc.a2 * fxx, mc.a1 * vi.y + mc.a2 * fyy,
+                    mc.a1 * vi.z + mc.a2 * fzz, 0.f);
+  s.incr[b] = inc;
+  const float4 xo = s.x[cur][b];
+  s.x[cur ^ 1][b] = make_float4(xo.x + inc.x, xo.y + inc.y, xo.z + inc.z, xo.w);
+  const float4 pi = s.p[cur][b];
+  const float boxl = s.boxl;
+  s.p[cur ^ 1][b] = make_float4(min_image(pi.x + inc.x, boxl), min_image(pi.y + inc.y, boxl),
                                 min_image(pi.z + inc.z, boxl), 0.f);
 }
 
@@ -215,8 +236,9 @@ __global__ void __launch_bounds__(256) k_energy(DevSys s, int mol_start, int mol
       const float4 xj = X[s.bond_j[br.x + e]];
       const float r0 = s.bond_r0[br.x + e];
       float lx, ly, lz;
-      float dx = diff_exact(xj.x, xi.x, boxl, lx), dy = diff_exact(xj.y, xi.y, boxl, ly),
-            dz = diff_exact(xj.z, xi.z, boxl, lz);
+      float dx = diff_exact(xj.x, xi.x, lx), dy = diff_exact(xj.y, xi.y, ly),
+            dz = diff_exact(xj.z, xi.z, lz);
+      min_image3(dx, dy, dz, boxl);
       float r = sqrtf(dx * dx + dy * dy + dz * dz);
       float dev = d2_minus_r02(dx, dy, dz, lx, ly, lz, r0) / (r + r0);
       eb += log1pf(-dev * dev / s.R0sq);
@@ -224,8 +246,8 @@ __global__ void __launch_bounds__(256) k_energy(DevSys s, int mol_start, int mol
     const int2 ar = s.ang_row[i];
     for (int e = 0; e < ar.y; ++e) {
       const float4 xj = X[s.ang_j[ar.x + e]];
-      float dx = min_image(xj.x - xi.x, boxl), dy = min_image(xj.y - xi.y, boxl),
-            dz = min_image(xj.z - xi.z, boxl);
+      float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
+      min_image3(dx, dy, dz, boxl);
       float inv = 1.0f / (dx * dx + dy * dy + dz * dz);
       ea += s.e_ss * inv * inv * inv;
     }
@@ -234,8 +256,9 @@ __global__ void __launch_bounds__(256) k_energy(DevSys s, int mol_start, int mol
       const float4 q = s.pl_att[abase + e];
       const float4 xj = X[__float_as_int(q.x)];
       float lx, ly, lz;
-      float dx = diff_exact(xj.x, xi.x, boxl, lx), dy = diff_exact(xj.y, xi.y, boxl, ly),
-            dz = diff_exact(xj.z, xi.z, boxl, lz);
+      float dx = diff_exact(xj.x, xi.x, lx), dy = diff_exact(xj.y, xi.y, ly),
+            dz = diff_exact(xj.z, xi.z, lz);
+      min_image3(dx, dy, dz, boxl);
       float d2 = dx * dx + dy * dy + dz * dz;
       float sr = q.y * q.y / d2;
       float s3 = sr * sr * sr;
@@ -248,8 +271,8 @@ __global__ void __launch_bounds__(256) k_energy(DevSys s, int mol_start, int mol
     const int ti = type_of(xi);
     for (int e = 0; e < rcnt; ++e) {
       const float4 xj = X[s.pl_j[rbase + e]];
-      float dx = min_image(xj.x - xi.x, boxl), dy = min_image(xj.y - xi.y, boxl),
-            dz = min_image(xj.z - xi.z, boxl);
+      float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
+      min_image3(dx, dy, dz, boxl);
       float u = s.sig2[ti][type_of(xj)] / (dx * dx + dy * dy + dz * dz);
       float u3 = u * u * u;
       erp += s.rep6 ? s.eps_rep * u3 : s.eps_rep * u3 * (u3 + 1.0f);
@@ -301,9 +324,9 @@ __global__ void __launch_bounds__(256) k_observables(DevSys s, int mol_start, in
       int j = s.nat_j[nr.x + e];
       if (j < i) continue;
       const float4 xj = X[j];
-      float dx = min_image(__fsub_rn(xi.x, xj.x), s.boxl);
-      float dy = min_image(__fsub_rn(xi.y, xj.y), s.boxl);
-      float dz = min_image(__fsub_rn(xi.z, xj.z), s.boxl);
+      float dx = __fsub_rn(xi.x, xj.x), dy = __fsub_rn(xi.y, xj.y),
+            dz = __fsub_rn(xi.z, xj.z);
+      min_image3(dx, dy, dz, s.boxl);
       float d = sqrtf(d2_exact(dx, dy, dz));
       if (__fdiv_rn(d, s.nat_par[nr.x + e].x) < 1.25f) ++cnt;
     }
@@ -343,29 +366,40 @@ __global__ void k_observables_final(const double* __restrict__ part, int nblocks
   out[3] = t[0];                                               // contct_nat
 }
 
+// Every bead's current unwrapped coordinates (each molecule at its own step
+// parity) in bead-id order, for one device-to-host copy.
+__global__ void k_gather_current(DevSys s, float4* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.nbead) return;
+  int m = s.mol_of[i];
+  out[i] = m < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : s.x[(int)(s.mol_step[m] & 1)][i];
+}
+
 // ----------------------------------------------------------- launchers
 static inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
 template <int G>
-static void launch_step_g(const DevSys& s, const int2* tiles, int ntiles, int koff, bool step,
-                          cudaStream_t st) {
-  if (ntiles <= 0) return;
+static void launch_step_g(const DevSys& s, int koff, bool step, cudaStream_t st) {
+  const unsigned blocks = cdiv(s.nbead, 256 / G);
   if (step)
-    k_step<G, true><<<ntiles, 256, 0, st>>>(s, tiles, koff);
+    k_step<G, true><<<blocks, 256, 0, st>>>(s, koff);
   else
-    k_step<G, false><<<ntiles, 256, 0, st>>>(s, tiles, koff);
+    k_step<G, false><<<blocks, 256, 0, st>>>(s, koff);
 }
 
-void launch_step(const DevSys& s, int G, const int2* tiles, int ntiles, int koff, bool step,
-                 cudaStream_t st) {
+void launch_step(const DevSys& s, int G, int koff, bool step, cudaStream_t st) {
   switch (G) {
-    case 1: launch_step_g<1>(s, tiles, ntiles, koff, step, st); break;
-    case 2: launch_step_g<2>(s, tiles, ntiles, koff, step, st); break;
-    case 4: launch_step_g<4>(s, tiles, ntiles, koff, step, st); break;
-    case 8: launch_step_g<8>(s, tiles, ntiles, koff, step, st); break;
-    case 16: launch_step_g<16>(s, tiles, ntiles, koff, step, st); break;
-    default: launch_step_g<32>(s, tiles, ntiles, koff, step, st); break;
+    case 1: launch_step_g<1>(s, koff, step, st); break;
+    case 2: launch_step_g<2>(s, koff, step, st); break;
+    case 4: launch_step_g<4>(s, koff, step, st); break;
+    case 8: launch_step_g<8>(s, koff, step, st); break;
+    case 16: launch_step_g<16>(s, koff, step, st); break;
+    default: launch_step_g<32>(s, koff, step, st); break;
   }
+}
+
+void launch_gather_current(const DevSys& s, float4* out, cudaStream_t st) {
+  k_gather_current<<<cdiv(s.nbead, 256), 256, 0, st>>>(s, out);
 }
 
 void launch_advance(const DevSys& s, int steps, cudaStream_t st) {

@@ -65,6 +65,7 @@ struct DevSys {
   float rc2_pl_rep[3][3];
   float rc_nl_rep_max;          // max neighbour-list cut-off (A)
   float sig2[3][3];             // sigma_rep^2 by type pair
+  float rep_tol[3][3];          // sigma_rep * 1e-7: pairs with d^2 <= this are skipped (energy.cu:555-558)
   unsigned seed_lo, seed_hi;
 
   float4* x[2];
@@ -119,6 +120,18 @@ __device__ __forceinline__ float min_image(float d, float boxl) {
   return d;
 }
 
+// Minimum image of a whole separation vector with one branch: the exact
+// division runs only when some component exceeds boxl/4 (never for pairs on
+// the lists of a molecule smaller than the box), so the common path is three
+// compares.  Same results as min_image on each component.
+__device__ __forceinline__ void min_image3(float& dx, float& dy, float& dz, float boxl) {
+  if (fmaxf(fabsf(dx), fmaxf(fabsf(dy), fabsf(dz))) > 0.25f * boxl) {
+    dx = min_image(dx, boxl);
+    dy = min_image(dy, boxl);
+    dz = min_image(dz, boxl);
+  }
+}
+
 // FP32 squared distance formed left to right without fused multiply-adds,
 // the arithmetic of the reference's host list filters (sop.cu:1378-1386):
 // list membership decided on it is bit-exact with the oracle.
@@ -156,11 +169,11 @@ __device__ __forceinline__ float d2_minus_r02(float dx, float dy, float dz, floa
   return __fadd_rn(hi, __fsub_rn(lo, qe));
 }
 
-// a - b as hi + lo exactly (two-sum of a and -b), hi minimum-imaged.
-__device__ __forceinline__ float diff_exact(float a, float b, float boxl, float& lo) {
+// a - b as hi + lo exactly (two-sum of a and -b); the caller minimum-images hi.
+__device__ __forceinline__ float diff_exact(float a, float b, float& lo) {
   float hi;
   two_sum(a, -b, hi, lo);
-  return min_image(hi, boxl);
+  return hi;
 }
 
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).

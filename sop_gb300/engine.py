@@ -89,12 +89,17 @@ def lib() -> ctypes.CDLL:
             "sop_upload_topology": (I, [V, ctypes.POINTER(MoleculeDesc)]),
             "sop_upload_state": (I, [V, I, V, V, V]),
             "sop_step": (I, [V, LL]),
+            "sop_step_async": (I, [V, LL]),
+            "sop_sync": (I, [V]),
+            "sop_launch_stage": (I, [V, I, I]),
             "sop_update_neighbor_list": (I, [V, PLL, PLL]),
             "sop_update_pair_list": (I, [V, PLL, PLL]),
             "sop_force_eval": (I, [V]),
             "sop_set_noise": (I, [V, V]),
             "sop_download": (I, [V, I, V, V, V, V]),
             "sop_download_list": (I, [V, I, I, LL, V, V, V, PLL]),
+            "sop_list_sizes": (I, [V, V]),
+            "sop_download_all": (I, [V, V]),
             "sop_energy": (I, [V, I, V]),
             "sop_observables": (I, [V, I, V]),
             "sop_molecule_status": (I, [V, I, ctypes.POINTER(I), PLL]),
@@ -193,6 +198,15 @@ class Engine:
     def step(self, n: int) -> None:
         self._check(lib().sop_step(self.h, int(n)), self.h)
 
+    def step_async(self, n: int) -> None:
+        self._check(lib().sop_step_async(self.h, int(n)), self.h)
+
+    def sync(self) -> None:
+        self._check(lib().sop_sync(self.h), self.h)
+
+    def launch_stage(self, stage: int, koff: int = 0) -> None:
+        self._check(lib().sop_launch_stage(self.h, int(stage), int(koff)), self.h)
+
     def force_eval(self) -> None:
         self._check(lib().sop_force_eval(self.h), self.h)
 
@@ -237,6 +251,21 @@ class Engine:
         self._check(lib().sop_download_list(self.h, mol, which, k, _p(i), _p(j), _p(r0),
                                             ctypes.byref(cnt)), self.h)
         return i[:k], j[:k], r0[:k]
+
+    def list_sizes(self) -> dict:
+        o = np.zeros(4, np.int64)
+        self._check(lib().sop_list_sizes(self.h, _p(o)), self.h)
+        return {"nnl_att": int(o[0]), "nnl_rep": int(o[1]), "nil_att": int(o[2]),
+                "nil_rep": int(o[3])}
+
+    def download_all(self, out: np.ndarray | None = None) -> np.ndarray:
+        """Coordinates of every bead, molecules in id order, shape (total, 3)."""
+        total = sum(m.n for m in self.mols)
+        if out is None:
+            out = np.empty((total, 3), np.float32)
+        assert out.dtype == np.float32 and out.flags.c_contiguous and out.size == 3 * total
+        self._check(lib().sop_download_all(self.h, _p(out)), self.h)
+        return out
 
     def energy(self, mol: int = 0) -> np.ndarray:
         t = np.zeros(5, np.float64)
