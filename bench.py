@@ -291,6 +291,7 @@ def main() -> None:
         e.step_async(MD_STEPS)
     e.sync()
     s_start = e.status(0)[1]
+    tuning = e.tuning()
 
     K = args.steps
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -411,6 +412,7 @@ def main() -> None:
             "plain_loop": plain,
             "batched_over_plain": (value / world / plain["value"]) if plain else None,
             "lists": ls,
+            "tuning": tuning,
             "molecule_errors": int(sum(1 for s in statuses if s & 3)),
         }
         print(json.dumps(line), flush=True)

@@ -221,6 +221,12 @@ int sop_molecule_status(void* ctx, int mol, int* status, long long* step);
 /* Total device bytes held by the context, and the bytes charged to `mol`. */
 int sop_memory(void* ctx, int mol, long long* ctx_bytes, long long* mol_bytes);
 
+/* Lanes per bead the step kernel uses (chosen at sop_commit by timing 2, 4, 8
+ * and 16 unless sop_params.lanes_per_bead fixed it) and the measured kernel
+ * times in ms for those four candidates (0 when not tuned).  Forces are
+ * bit-identical for every choice. */
+int sop_tuning(void* ctx, int* lanes, float* ms);
+
 /* The context's CUDA stream (a cudaStream_t), for callers that time or order
  * work around the engine. */
 int sop_stream(void* ctx, void** stream);

@@ -103,6 +103,7 @@ struct SopCtx {
   double* e_out = nullptr;    // 8 doubles
   double* h_out = nullptr;    // pinned copy of e_out
   float4* stage = nullptr;    // gather buffer of sop_download_all
+  std::map<int, float> tuning;  // step-kernel time (ms) per lanes-per-bead candidate
   long long host_step = 0;    // common step of plain / batched contexts
   long long target_step = 0;  // step every molecule should reach after the queued work
   std::map<std::string, Graph> graphs;
@@ -166,8 +167,36 @@ namespace {
 
 int lanes_for(const SopCtx* ctx) {
   int g = ctx->P.lanes_per_bead;
-  if (g == 1 || g == 2 || g == 4 || g == 8 || g == 16 || g == 32) return g;
-  return 8;
+  if (g == 2 || g == 4 || g == 8 || g == 16) return g;
+  return 0;  // autotune
+}
+
+// Picks the lanes per bead G of the step kernel for this context by timing
+// the force-only kernel (idempotent: it recomputes the same forces and
+// look-ahead from the same state) for each G; results are bit-identical for
+// every G, so only the speed differs.
+int autotune_lanes(SopCtx* ctx) {
+  const int cand[4] = {2, 4, 8, 16};
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  float best = 1e30f;
+  int bestg = 8;
+  for (int g : cand) {
+    launch_step(ctx->s, g, 0, false, ctx->stream);  // warm-up
+    CK(cudaEventRecord(a, ctx->stream));
+    for (int r = 0; r < 3; ++r) launch_step(ctx->s, g, 0, false, ctx->stream);
+    CK(cudaEventRecord(b, ctx->stream));
+    CK(cudaEventSynchronize(b));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, a, b));
+    ctx->tuning[g] = ms / 3.0f;
+    if (ms < best) { best = ms; bestg = g; }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  ctx->G = bestg;
+  return SOP_OK;
 }
 
 // (Re)allocates the fixed-stride neighbour / pair-list rows.
@@ -355,6 +384,7 @@ int commit(SopCtx* ctx) {
   s.k_bnd = (float)P.k_bnd;
   s.R0 = (float)P.R0;
   s.R0sq = (float)(P.R0 * P.R0);
+  s.inv_R0sq = (float)(1.0 / (P.R0 * P.R0));
   double sig6 = std::pow(P.sigma_ss, 6.0);
   s.f_ss = (float)(6.0 * P.eps_ss * sig6);
   s.e_ss = (float)(P.eps_ss * sig6);
@@ -434,6 +464,10 @@ int commit(SopCtx* ctx) {
       cell_cap += std::max<long long>(64, 2LL * m.n);
     }
   }
+  s.uniform_type = 1;
+  for (auto& m : ctx->mols)
+    for (int t : m.types)
+      if (t != 1) s.uniform_type = 0;
   ctx->mc.resize(nmol);
   for (int mi = 0; mi < nmol; ++mi) ctx->mc[mi] = make_const(P, ctx->mols[mi]);
 
@@ -533,13 +567,18 @@ int commit(SopCtx* ctx) {
   CK(cudaMemsetAsync(s.pl_cnt, 0, sizeof(int) * nb, st));
   CK(cudaMemsetAsync(s.nl_maxrow, 0, sizeof(int), st));
 
-  ctx->G = lanes_for(ctx);
+  const int fixed_g = lanes_for(ctx);
+  ctx->G = fixed_g ? fixed_g : 8;
   // set-up of underdamped_ctrl: lists from x_0, then f_0 and the look-ahead
   int rc = nl_rebuild_checked(ctx, 0);
   if (rc) return rc;
   launch_pl_rebuild(s, 0, st);
   force_eval_async(ctx);
   CK(cudaGetLastError());
+  if (!fixed_g) {
+    rc = autotune_lanes(ctx);
+    if (rc) return rc;
+  }
   CK(cudaStreamSynchronize(st));
   ctx->host_step = 0;
   ctx->target_step = 0;
@@ -1031,6 +1070,20 @@ int sop_memory(void* p, int mol, long long* ctx_bytes, long long* mol_bytes) {
     long long nl = ctx->s.nl_stride * 8LL * hm.n;
     *mol_bytes = per_bead * hm.n + nl + (long long)(hm.bi.size() + hm.ai.size()) * 16 +
                  (long long)hm.ni.size() * 2 * 40;
+  }
+  return SOP_OK;
+}
+
+int sop_tuning(void* p, int* lanes, float* ms) {
+  if (!p) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (lanes) *lanes = ctx->G;
+  if (ms) {
+    const int cand[4] = {2, 4, 8, 16};
+    for (int k = 0; k < 4; ++k) {
+      auto it = ctx->tuning.find(cand[k]);
+      ms[k] = it == ctx->tuning.end() ? 0.0f : it->second;
+    }
   }
   return SOP_OK;
 }

@@ -5,10 +5,11 @@
 // The reference runs per step underdamped_iteration_kernel (sop.cu:421-447),
 // clear_forces + rand_kernel + four force kernels with float atomics
 // (energy.cu:54-167, 228-584) and update_velocities_kernel (sop.cu:450-462).
-// Here a group of G lanes owns a bead: it sums the bead's force over its own
-// full rows (every pair is stored for both beads), reduces across the group
-// with shuffles, adds the noise, and updates velocity and coordinates.  No
-// atomics; the summation order is fixed by G and the row order.
+// Here a group of G lanes owns a bead (beads taken in cell order, so
+// neighbouring groups gather from the same region): it sums the bead's force
+// over its own full rows (every pair is stored for both beads) in an order
+// that does not depend on G, then one thread per bead adds the noise and
+// updates velocity and coordinates.  No atomics.
 //
 // Step bookkeeping: kernel K_n computes f_n = F(x_n) + noise(n), then
 // v_n = a3 incr_n + a4 f_n, then the look-ahead incr_{n+1} = a1 v_n + a2 f_n
@@ -21,16 +22,11 @@
 
 namespace sop {
 
-template <int G>
-__device__ __forceinline__ float group_sum(float v, unsigned gmask) {
-#pragma unroll
-  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(gmask, v, o);
-  return v;
-}
+constexpr int kV = 16;  // virtual lanes of the fixed force-summation order
 
 // STEP = false: force evaluation only at step mol_step + koff (velocities kept),
 // followed by the look-ahead; used after set-up and state uploads.
-template <int G, bool STEP>
+template <int G, bool STEP, bool UNI>
 __global__ void __launch_bounds__(256) k_step(DevSys s, int koff) {
   constexpr int BPB = 256 / G;          // beads per block
   __shared__ float4 fsum[BPB];          // conservative force sums; w = FENE range flag
@@ -48,7 +44,16 @@ __global__ void __launch_bounds__(256) k_step(DevSys s, int koff) {
     n = s.mol_step[m] + (STEP ? 1 : 0) + koff;
     if (mc.active && s.mol_status[m] == 0 && !(STEP && mc.nsteps >= 0 && n > mc.nsteps)) i = b;
   }
-  float fx = 0.f, fy = 0.f, fz = 0.f;
+  // Forces are summed in a fixed order whatever G is: entry e of a row
+  // accumulates into virtual lane e % kV (in increasing e), and the kV partial
+  // sums combine in one fixed binary tree (pairs v, v + kV/2, then v, v + kV/4,
+  // ...).  Each physical lane holds kC = kV / G virtual lanes and does the
+  // upper tree levels locally, the rest by shuffles.  So every G gives
+  // bit-identical forces, and G is free to tune per context.
+  constexpr int kC = kV / G;
+  float ax[kC], ay[kC], az[kC];
+#pragma unroll
+  for (int c = 0; c < kC; ++c) ax[c] = ay[c] = az[c] = 0.f;
   bool fene_bad = false;
   if (i >= 0) {  // uniform over the lane group
     const unsigned gmask = (G == 32) ? 0xffffffffu
@@ -65,95 +70,122 @@ __global__ void __launch_bounds__(256) k_step(DevSys s, int koff) {
     const int rcnt = s.pl_cnt[i];
 
     // Bonded, angle and native terms share one index space [bonds | angles |
-    // natives]; a bead has a handful of them, usually one pass of the group.
+    // natives]; a bead has a handful of them, usually one pass.
     const int nba = br.y + ar.y;
     const int nsmall = nba + acnt;
-    for (int e = lane; e < nsmall; e += G) {
-      int j;
-      float r0 = 0.f, eps = 0.f;
-      if (e < br.y) {
-        j = s.bond_j[br.x + e];
-        r0 = s.bond_r0[br.x + e];
-      } else if (e < nba) {
-        j = s.ang_j[ar.x + e - br.y];
-      } else {
-        const float4 q = s.pl_att[abase + e - nba];
-        j = __float_as_int(q.x);
-        r0 = q.y;
-        eps = q.z;
+    for (int base = 0; base < nsmall; base += kV) {
+#pragma unroll
+      for (int c = 0; c < kC; ++c) {
+        const int e = base + lane + c * G;
+        if (e >= nsmall) continue;
+        int j;
+        float r0 = 0.f, eps = 0.f;
+        if (e < br.y) {
+          j = s.bond_j[br.x + e];
+          r0 = s.bond_r0[br.x + e];
+        } else if (e < nba) {
+          j = s.ang_j[ar.x + e - br.y];
+        } else {
+          const float4 q = s.pl_att[abase + e - nba];
+          j = __float_as_int(q.x);
+          r0 = q.y;
+          eps = q.z;
+        }
+        const float4 xj = X[j];
+        float lx, ly, lz;
+        float dx = diff_exact(xj.x, xi.x, lx), dy = diff_exact(xj.y, xi.y, ly),
+              dz = diff_exact(xj.z, xi.z, lz);
+        min_image3(dx, dy, dz, boxl);
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        float cc;
+        if (e < br.y) {
+          // FENE: force on i = +k dev / (r (1 - dev^2/R0^2)) * d  (energy.cu:252-271);
+          // dev carries the compensated d^2 - r0^2, so approximate reciprocals
+          // (a few ulps) keep the term well inside the force tolerance
+          const float r = d2 * rsqrtf(d2);
+          const float dev = d2_minus_r02(dx, dy, dz, lx, ly, lz, r0) * __fdividef(1.0f, r + r0);
+          const float w = 1.0f - dev * dev * s.inv_R0sq;
+          fene_bad |= !(fabsf(dev) < s.R0);
+          cc = s.k_bnd * dev * __fdividef(1.0f, r * w);
+        } else if (e < nba) {
+          // i,i+2 soft sphere: force on i = -6 eps sigma^6 / d^8 * d  (energy.cu:335-360)
+          const float inv = __fdividef(1.0f, d2);
+          const float inv2 = inv * inv;
+          cc = -s.f_ss * inv2 * inv2;
+        } else {
+          // native LJ 12-6 (energy.cu:468-507): co1 = -12 eps / d^2 (s^6 - s^3),
+          // s = r0^2 / d^2, as -12 eps / d^2 s^3 (s - 1)(s^2 + s + 1) with
+          // s - 1 = -(d^2 - r0^2) / d^2; pairs with d^2 <= 1e-7 r0^2 are skipped.
+          const float r02 = r0 * r0;
+          const float inv = __fdividef(1.0f, d2);
+          const float sr = r02 * inv;
+          const float sm1 = -d2_minus_r02(dx, dy, dz, lx, ly, lz, r0) * inv;
+          const float s3 = sr * sr * sr;
+          cc = (d2 > 1.0e-7f * r02) ? -12.0f * eps * inv * s3 * sm1 * (sr * sr + sr + 1.0f) : 0.0f;
+        }
+        ax[c] += cc * dx; ay[c] += cc * dy; az[c] += cc * dz;
       }
-      const float4 xj = X[j];
-      float lx, ly, lz;
-      float dx = diff_exact(xj.x, xi.x, lx), dy = diff_exact(xj.y, xi.y, ly),
-            dz = diff_exact(xj.z, xi.z, lz);
-      min_image3(dx, dy, dz, boxl);
-      const float d2 = dx * dx + dy * dy + dz * dz;
-      float c;
-      if (e < br.y) {
-        // FENE: force on i = +k dev / (r (1 - dev^2/R0^2)) * d  (energy.cu:252-271)
-        const float r = sqrtf(d2);
-        const float dev = d2_minus_r02(dx, dy, dz, lx, ly, lz, r0) / (r + r0);
-        const float w = 1.0f - dev * dev / s.R0sq;
-        fene_bad |= !(fabsf(dev) < s.R0);
-        c = s.k_bnd * dev / (r * w);
-      } else if (e < nba) {
-        // i,i+2 soft sphere: force on i = -6 eps sigma^6 / d^8 * d  (energy.cu:335-360)
-        const float inv = __fdividef(1.0f, d2);
-        const float inv2 = inv * inv;
-        c = -s.f_ss * inv2 * inv2;
-      } else {
-        // native LJ 12-6 (energy.cu:468-507): co1 = -12 eps / d^2 (s^6 - s^3),
-        // s = r0^2 / d^2, as -12 eps / d^2 s^3 (s - 1)(s^2 + s + 1) with
-        // s - 1 = -(d^2 - r0^2) / d^2; pairs with d^2 <= 1e-7 r0^2 are skipped.
-        const float r02 = r0 * r0;
-        const float inv = __fdividef(1.0f, d2);
-        const float sr = r02 * inv;
-        const float sm1 = -d2_minus_r02(dx, dy, dz, lx, ly, lz, r0) * inv;
-        const float s3 = sr * sr * sr;
-        c = (d2 > 1.0e-7f * r02) ? -12.0f * eps * inv * s3 * sm1 * (sr * sr + sr + 1.0f) : 0.0f;
-      }
-      fx += c * dx; fy += c * dy; fz += c * dz;
     }
 
     // Non-native repulsion (energy.cu:536-581): co1 = -6 eps / d^2 (2 (s/r)^12 +
     // (s/r)^6) [rep6: -6 eps / d^2 (s/r)^6]; pairs with d^2 <= 1e-7 sigma are
-    // skipped.  Each lane takes 4 consecutive entries per iteration (one
-    // 16-byte load of the row, four independent gathers); entries past the row
-    // end read bead i itself, which the tolerance test drops.
+    // skipped.  kC loads in flight per lane per chunk of kV entries.  A system
+    // of one bead type (UNI) uses its sigma as a constant.
     const int ti = type_of(xi);
     const float g11 = s.sig2[1][1], g12 = s.sig2[1][2], g22 = s.sig2[2][2];
     const float t11 = s.rep_tol[1][1], t12 = s.rep_tol[1][2], t22 = s.rep_tol[2][2];
     const float ce = -6.0f * s.eps_rep;
     const float two = s.rep6 ? 0.0f : 2.0f;
-    auto rep = [&](const float4 xj) {
-      float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
-      min_image3(dx, dy, dz, boxl);
-      const float d2 = dx * dx + dy * dy + dz * dz;
-      const int tj = type_of(xj);
-      const float sg2 = pick_type_pair(g11, g12, g22, ti, tj);
-      const float inv = __fdividef(1.0f, d2);
-      const float u = sg2 * inv;
-      const float u3 = u * u * u;
-      const float c = (d2 > pick_type_pair(t11, t12, t22, ti, tj)) ? ce * inv * u3 * (two * u3 + 1.0f) : 0.0f;
-      fx += c * dx; fy += c * dy; fz += c * dz;
-    };
-    const int4* prow = reinterpret_cast<const int4*>(s.pl_j + rbase);
-    for (int e = 4 * lane; e < rcnt; e += 4 * G) {
-      const int4 jv = prow[e >> 2];
-      const float4 x0 = X[jv.x];
-      const float4 x1 = X[e + 1 < rcnt ? jv.y : i];
-      const float4 x2 = X[e + 2 < rcnt ? jv.z : i];
-      const float4 x3 = X[e + 3 < rcnt ? jv.w : i];
-      rep(x0);
-      rep(x1);
-      rep(x2);
-      rep(x3);
+    const float q4 = 0.25f * boxl;
+    const int* __restrict__ prow = s.pl_j + rbase;
+    for (int base = 0; base < rcnt; base += kV) {
+      int jj[kC];
+#pragma unroll
+      for (int c = 0; c < kC; ++c) {
+        const int e = base + lane + c * G;
+        jj[c] = e < rcnt ? prow[e] : i;
+      }
+      float4 xx[kC];
+#pragma unroll
+      for (int c = 0; c < kC; ++c) xx[c] = X[jj[c]];
+#pragma unroll
+      for (int c = 0; c < kC; ++c) {
+        // past the row end xx[c] is bead i itself: d2 = 0 fails the tolerance
+        // test and contributes exactly 0, so no branch is needed
+        float dx = xx[c].x - xi.x, dy = xx[c].y - xi.y, dz = xx[c].z - xi.z;
+        // |dx| + |dy| + |dz| bounds every component: one test for the rare wrap
+        if (fabsf(dx) + fabsf(dy) + fabsf(dz) > q4) min_image3(dx, dy, dz, boxl);
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        float sg2 = g11, tol = t11;
+        if (!UNI) {
+          const int tj = type_of(xx[c]);
+          sg2 = pick_type_pair(g11, g12, g22, ti, tj);
+          tol = pick_type_pair(t11, t12, t22, ti, tj);
+        }
+        const float inv = __fdividef(1.0f, d2);
+        const float u = sg2 * inv;
+        const float u3 = u * u * u;
+        const float cc = (d2 > tol) ? ce * inv * u3 * (two * u3 + 1.0f) : 0.0f;
+        ax[c] += cc * dx; ay[c] += cc * dy; az[c] += cc * dz;
+      }
     }
-    fx = group_sum<G>(fx, gmask);
-    fy = group_sum<G>(fy, gmask);
-    fz = group_sum<G>(fz, gmask);
+    // upper levels of the fixed tree inside the lane, lower levels by shuffles
+#pragma unroll
+    for (int off = kV / 2; off >= G; off >>= 1) {
+      const int oc = off / G;
+#pragma unroll
+      for (int c = 0; c < kC; ++c)
+        if (c < oc) { ax[c] += ax[c + oc]; ay[c] += ay[c + oc]; az[c] += az[c + oc]; }
+    }
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) {
+      ax[0] += __shfl_xor_sync(gmask, ax[0], off);
+      ay[0] += __shfl_xor_sync(gmask, ay[0], off);
+      az[0] += __shfl_xor_sync(gmask, az[0], off);
+    }
     fene_bad = __any_sync(gmask, fene_bad);
   }
+  const float fx = ax[0], fy = ay[0], fz = az[0];
   if (lane == 0) {
     fsum[slot] = make_float4(fx, fy, fz, fene_bad ? 1.0f : 0.0f);
     bead[slot] = i;
@@ -381,20 +413,22 @@ static inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b
 template <int G>
 static void launch_step_g(const DevSys& s, int koff, bool step, cudaStream_t st) {
   const unsigned blocks = cdiv(s.nbead, 256 / G);
-  if (step)
-    k_step<G, true><<<blocks, 256, 0, st>>>(s, koff);
-  else
-    k_step<G, false><<<blocks, 256, 0, st>>>(s, koff);
+  if (s.uniform_type) {
+    if (step) k_step<G, true, true><<<blocks, 256, 0, st>>>(s, koff);
+    else k_step<G, false, true><<<blocks, 256, 0, st>>>(s, koff);
+  } else {
+    if (step) k_step<G, true, false><<<blocks, 256, 0, st>>>(s, koff);
+    else k_step<G, false, false><<<blocks, 256, 0, st>>>(s, koff);
+  }
 }
 
+// Lanes per bead G in {2, 4, 8, 16}.
 void launch_step(const DevSys& s, int G, int koff, bool step, cudaStream_t st) {
   switch (G) {
-    case 1: launch_step_g<1>(s, koff, step, st); break;
     case 2: launch_step_g<2>(s, koff, step, st); break;
     case 4: launch_step_g<4>(s, koff, step, st); break;
-    case 8: launch_step_g<8>(s, koff, step, st); break;
     case 16: launch_step_g<16>(s, koff, step, st); break;
-    default: launch_step_g<32>(s, koff, step, st); break;
+    default: launch_step_g<8>(s, koff, step, st); break;
   }
 }
 

@@ -58,7 +58,7 @@ struct DevSys {
   float boxl;
   float eps_rep;
   int rep6;
-  float k_bnd, R0sq, R0;
+  float k_bnd, R0sq, R0, inv_R0sq;
   float f_ss;                   // 6 eps_ss sigma_ss^6 (param.cpp:36-39)
   float e_ss;                   // eps_ss sigma_ss^6
   float rc2_nl_rep[3][3];       // squared cut-offs by type pair
@@ -66,6 +66,7 @@ struct DevSys {
   float rc_nl_rep_max;          // max neighbour-list cut-off (A)
   float sig2[3][3];             // sigma_rep^2 by type pair
   float rep_tol[3][3];          // sigma_rep * 1e-7: pairs with d^2 <= this are skipped (energy.cu:555-558)
+  int uniform_type;             // 1: every bead has type 1 (one sigma for all pairs)
   unsigned seed_lo, seed_hi;
 
   float4* x[2];

@@ -104,6 +104,7 @@ def lib() -> ctypes.CDLL:
             "sop_observables": (I, [V, I, V]),
             "sop_molecule_status": (I, [V, I, ctypes.POINTER(I), PLL]),
             "sop_memory": (I, [V, I, PLL, PLL]),
+            "sop_tuning": (I, [V, ctypes.POINTER(I), V]),
             "sop_stream": (I, [V, ctypes.POINTER(V)]),
             "sop_last_error": (ctypes.c_char_p, [V]),
         }
@@ -287,6 +288,13 @@ class Engine:
         a, b = ctypes.c_longlong(), ctypes.c_longlong()
         self._check(lib().sop_memory(self.h, mol, ctypes.byref(a), ctypes.byref(b)), self.h)
         return a.value, b.value
+
+    def tuning(self) -> dict:
+        g = ctypes.c_int()
+        ms = np.zeros(4, np.float32)
+        self._check(lib().sop_tuning(self.h, ctypes.byref(g), _p(ms)), self.h)
+        return {"lanes_per_bead": g.value,
+                "ms": {str(k): float(v) for k, v in zip((2, 4, 8, 16), ms)}}
 
     def stream(self) -> int:
         s = ctypes.c_void_p()

@@ -1,0 +1,105 @@
+"""The oracle, the file readers and the generator pinned against fixtures made
+by the reference's own host routines (tests/golden/make_golden.py)."""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+from sop_gb300 import system
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _files(prefix):
+    return [f"{prefix}.{k}" for k in ("bonds", "angles", "vdw", "init")]
+
+
+def test_reader_matches_reference_loader():
+    g = np.load(os.path.join(GOLD, "m64_load.npz"))
+    m = system.read_reference_files(*_files(os.path.join(GOLD, "m64")))
+    nbead, nbnd, nang, natt, nrep = (int(v) for v in g["sizes"][:5])
+    assert (m.n, len(m.bond_i), len(m.ang_i), len(m.nat_i), m.n_rep_master) == \
+        (nbead, nbnd, nang, natt, nrep)
+    np.testing.assert_array_equal(m.bond_i, g["bi"])
+    np.testing.assert_array_equal(m.bond_j, g["bj"])
+    np.testing.assert_array_equal(m.bond_r0, g["br0"])
+    np.testing.assert_array_equal(m.ang_i, g["ai"])
+    np.testing.assert_array_equal(m.ang_k, g["ak"])
+    # the reference keeps file order; ours is (i, j)-sorted with i < j
+    ref_nat = sorted(zip(np.minimum(g["ni"], g["nj"]).tolist(), np.maximum(g["ni"], g["nj"]).tolist(),
+                         g["nr0"].tolist()))
+    ours = list(zip(m.nat_i.tolist(), m.nat_j.tolist(), m.nat_r0.tolist()))
+    assert ours == ref_nat
+    np.testing.assert_array_equal(m.xyz, g["unc"])
+    assert set(g["nti"].tolist()) == {1} and set(g["rti"].tolist()) == {1}
+    # the reference's non-native master list is exactly our implicit complement
+    ri, rj = system.rep_master(m)
+    assert set(zip(ri.tolist(), rj.tolist())) == set(zip(g["ri"].tolist(), g["rj"].tolist()))
+
+
+def test_generator_reproduces_committed_files():
+    m = system.generate(64, 11)
+    with tempfile.TemporaryDirectory() as d:
+        system.write_reference_files(m, os.path.join(d, "m64"))
+        for k in ("bonds", "angles", "vdw", "init"):
+            assert open(os.path.join(d, f"m64.{k}")).read() == \
+                open(os.path.join(GOLD, f"m64.{k}")).read(), k
+
+
+@pytest.mark.parametrize("mode", ["factor", "absolute"])
+def test_oracle_energies_match_reference(mode):
+    g = np.load(os.path.join(GOLD, "m128_energy.npz"))
+    m = system.generate(128, 0)
+    x = g["x"]
+    att = g[f"{mode}_att"]
+    # the reference's host energy uses coeff_att[1][1] = 0.7 for native pairs
+    # of type (1, 1) (global.cpp:51-55); its force uses 1.0 (energy.cu:3-7)
+    eps_e = np.full(len(m.nat_i), float(g["coeff_att_11"]), np.float32)
+    _, e = O.forces_f64(m, x, att, g[f"{mode}_rep_i"], g[f"{mode}_rep_j"], eps_energy=eps_e)
+    np.testing.assert_allclose(e, g[f"{mode}_energy"], rtol=2e-5, atol=1e-5)
+
+
+def test_oracle_lists_reproduce_fixture_lists():
+    g = np.load(os.path.join(GOLD, "m128_energy.npz"))
+    m = system.generate(128, 0)
+    x = g["x"]
+    att = O.filter_att(m, x, None, 3.2, 0.0)
+    ri, rj = O.nl_rep(m, x, 3.2, 0.0)
+    np.testing.assert_array_equal(O.filter_att(m, x, att, 2.5, 0.0), g["factor_att"])
+    pi, pj = O.filter_rep(m, x, ri, rj, 2.5, 0.0)
+    np.testing.assert_array_equal(pi, g["factor_rep_i"])
+    np.testing.assert_array_equal(pj, g["factor_rep_j"])
+
+
+def test_oracle_observables_match_reference():
+    g = np.load(os.path.join(GOLD, "m128_energy.npz"))
+    m = system.generate(128, 0)
+    ob = O.observables(m, g["x"], g["v"])
+    q, rg, kin, cnt = g["observables"]
+    assert ob["contct_nat"] == int(cnt)
+    assert ob["Q"] == pytest.approx(q, abs=1e-7)
+    assert ob["rgsq"] == pytest.approx(rg, rel=2e-6)
+    assert ob["kinT"] == pytest.approx(kin, rel=2e-6)
+
+
+def test_oracle_forces_are_the_energy_gradient():
+    """The force kernels exist in the reference only as CUDA; their FP64
+    restatement must be minus the gradient of the (pinned) energy."""
+    g = np.load(os.path.join(GOLD, "m128_energy.npz"))
+    m = system.generate(128, 0)
+    x = g["x"].astype(np.float32)
+    att, ri, rj = g["absolute_att"], g["absolute_rep_i"], g["absolute_rep_j"]
+    f, _ = O.forces_f64(m, x, att, ri, rj)
+    h = np.float32(2.0 ** -12)
+    rng = np.random.default_rng(3)
+    for idx in rng.choice(3 * m.n, 40, replace=False):
+        b, c = divmod(int(idx), 3)
+        xp, xm = x.copy(), x.copy()
+        xp[b, c] += h
+        xm[b, c] -= h
+        _, ep = O.forces_f64(m, xp, att, ri, rj)
+        _, em = O.forces_f64(m, xm, att, ri, rj)
+        fd = -(ep.sum() - em.sum()) / (float(xp[b, c]) - float(xm[b, c]))
+        assert fd == pytest.approx(f[b, c], rel=2e-4, abs=2e-5), (b, c)

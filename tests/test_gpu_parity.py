@@ -112,6 +112,25 @@ def test_energy_vs_fp64(mode):
     np.testing.assert_allclose(t[4], eo.sum(), rtol=2e-5)
 
 
+@pytest.mark.parametrize("mode", ["factor", "absolute"])
+def test_energy_and_observables_vs_reference_golden(mode):
+    """GPU energies and observables against the reference's own host routines
+    (fixtures of tests/golden/make_golden.py), with the reference's energy
+    coefficient for native pairs (coeff_att[1][1] = 0.7, global.cpp:51-55)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "m128_energy.npz"))
+    mol = mol_of(128, 0)
+    eps_e = np.full(len(mol.nat_i), float(g["coeff_att_11"]), np.float32)
+    with engine.plain(mol, g["x"], params(mode), vel=g["v"], eps_energy=eps_e) as e:
+        t = e.energy()
+        ob = e.observables()
+    np.testing.assert_allclose(t[:4], g[f"{mode}_energy"], rtol=2e-5, atol=1e-5)
+    q, rg, kin, cnt = g["observables"]
+    assert ob["contct_nat"] == int(cnt)
+    assert ob["rgsq"] == pytest.approx(rg, rel=2e-6)
+    assert ob["kinT"] == pytest.approx(kin, rel=2e-6)
+
+
 def test_observables_vs_fp64():
     mol = mol_of(4000, 1)
     x = perturbed(mol, 1.0, 4)
@@ -246,6 +265,55 @@ def test_batched_equals_alone():
             d = e.download(k)
             for key in ("unc_pos", "vel", "force"):
                 np.testing.assert_array_equal(d[key], alone[k][key])
+
+
+def test_lanes_per_bead_bit_identical():
+    """The force summation order does not depend on the lanes per bead, so
+    trajectories are bit-identical for every G (and G can be tuned freely)."""
+    mol = mol_of(4000, 1)
+    outs = []
+    for g in (2, 4, 8, 16):
+        p = engine.baseline_params(lanes_per_bead=g)
+        with engine.plain(mol, mol.xyz, p, T=0.6, traj=2) as e:
+            assert e.tuning()["lanes_per_bead"] == g
+            e.step(30)
+            outs.append(e.download())
+    for o in outs[1:]:
+        for k in ("unc_pos", "vel", "force"):
+            np.testing.assert_array_equal(o[k], outs[0][k])
+
+
+def test_autotune_picks_a_candidate():
+    mol = mol_of(4000, 1)
+    with engine.plain(mol, mol.xyz, engine.baseline_params()) as e:
+        t = e.tuning()
+    assert t["lanes_per_bead"] in (2, 4, 8, 16)
+    assert all(v > 0 for v in t["ms"].values())
+
+
+@pytest.mark.parametrize("mode", ["factor", "absolute"])
+def test_two_bead_types(mode):
+    """Type-2 beads use sigma_rep 7.0 (5.4 across types, energy.cu:9-13) in the
+    repulsion and in the list cut-offs."""
+    base = mol_of(1500, 4)
+    rng = np.random.default_rng(6)
+    types = np.where(rng.random(base.n) < 0.3, 2, 1).astype(np.int32)
+    mol = system.Molecule(base.n, base.xyz, base.bond_i, base.bond_j, base.bond_r0, base.ang_i,
+                          base.ang_j, base.ang_k, base.ang_r, base.nat_i, base.nat_j, base.nat_r0,
+                          base.nat_eps, types=types)
+    x = perturbed(mol, 0.2, 8)
+    p = params(mode)
+    with engine.plain(mol, x, p) as e:
+        e.set_noise(np.zeros((mol.n, 3), np.float32))
+        e.force_eval()
+        f = e.download()["force"]
+        _, (ri, rj), _, (pri, prj) = gpu_lists(e, mol)
+        pai, paj, _ = e.list_pairs(0, 2)
+    _, (nri, nrj), _, (opi, opj) = oracle_lists(mol, x, p)
+    assert pairset(ri, rj) == pairset(nri, nrj)
+    assert pairset(pri, prj) == pairset(opi, opj)
+    fo, _ = O.forces_f64(mol, x, att_sel(mol, pai, paj), pri, prj)
+    assert force_error(f, fo) <= FORCE_TOL
 
 
 def test_fene_range_is_flagged():
