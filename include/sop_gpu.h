@@ -231,6 +231,37 @@ int sop_tuning(void* ctx, int* lanes, float* ms);
  * work around the engine. */
 int sop_stream(void* ctx, void** stream);
 
+/*
+ * Serving (continuous batching).  No counterpart in the reference, which
+ * runs one molecule per process (sop.cu:13-55).  A served context holds
+ * device pools sized by an HBM budget (coordinates, velocities, topology,
+ * neighbour and pair lists, Philox counters are implicit) and runs jobs --
+ * molecules with step budgets -- that are submitted while others run.  Each
+ * sop_serve_advance round: wait for the previous round, retire finished or
+ * failed jobs (results copied to the host, slots freed), admit queued jobs in
+ * arrival order while their beads, topology and list rows fit the pools, then
+ * queue nnlup more steps of every active job.  An admitted job starts at the
+ * round's neighbour-list rebuild, so its own step count keeps the reference's
+ * cadence, and its trajectory is bit-identical to the same job run alone.
+ */
+int sop_serve_create(const sop_params* p, long long budget_bytes, long long max_job_beads,
+                     void** ctx);
+/* Queues a job (m->nsteps must be >= 0); *job receives its id. */
+int sop_serve_submit(void* ctx, const sop_molecule* m, int* job);
+/* Runs `rounds` rounds; returns when their work is queued on the device. */
+int sop_serve_advance(void* ctx, int rounds);
+/* Ids of jobs finished since the previous call (up to cap); *count receives
+ * how many were written. */
+int sop_serve_finished(void* ctx, int cap, int* jobs, int* count);
+/* Results of a finished job: coordinates and velocities (3*nbead floats, NULL
+ * skips), energy terms as sop_energy (5 doubles), SOP_MOL_* status, steps
+ * completed and the seconds from submission to retirement. */
+int sop_serve_result(void* ctx, int job, float* unc_pos, float* vel, double* energy,
+                     int* status, long long* steps, double* latency_s);
+/* out[0..7]: queued, active, finished jobs; active beads; bead capacity;
+ * device bytes held; budget; the context's step clock. */
+int sop_serve_stats(void* ctx, long long* out);
+
 /* Last error message of the context (or of the library when ctx is NULL). */
 const char* sop_last_error(void* ctx);
 

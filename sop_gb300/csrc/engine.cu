@@ -9,10 +9,13 @@
 // per-step loop body of underdamped_ctrl (sop.cu:197-243).
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <map>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -53,7 +56,58 @@ struct HostMol {
   double T = 0.6;
   unsigned traj = 0;
   long long nsteps = -1;
-  int start = 0;
+  int start = -1;                 // first bead slot; -1: not on the device
+  int slot = -1;                  // molecule slot
+  long long off_b = 0, off_a = 0, off_n = 0;  // topology pool offsets
+};
+
+// Capacities of the device pools.
+struct Caps {
+  long long beads = 0, mols = 0, bonds = 0, angles = 0, natives = 0, cells = 0;
+  long long max_mol_beads = 0, stride = 64;
+};
+
+// First-fit allocator of ranges in [0, cap), coalescing on release.
+struct RangeAlloc {
+  long long cap = 0;
+  std::map<long long, long long> free_;  // start -> length
+  void reset(long long c) {
+    cap = c;
+    free_.clear();
+    if (c > 0) free_[0] = c;
+  }
+  long long alloc(long long n) {
+    if (n <= 0) return 0;
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second < n) continue;
+      long long st = it->first, len = it->second;
+      free_.erase(it);
+      if (len > n) free_[st + n] = len - n;
+      return st;
+    }
+    return -1;
+  }
+  void release(long long st, long long n) {
+    if (n <= 0) return;
+    auto it = free_.emplace(st, n).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_.erase(it);
+      }
+    }
+  }
+  long long largest() const {
+    long long m = 0;
+    for (auto& kv : free_) m = std::max(m, kv.second);
+    return m;
+  }
 };
 
 // sigma_rep[itype][jtype] (energy.cu:9-13)
@@ -85,6 +139,26 @@ struct Graph {
   cudaGraphExec_t e = nullptr;
 };
 
+// A served job: queued (its molecule on the host), active (in a molecule
+// slot) or finished (its results on the host).
+struct Job {
+  enum { QUEUED = 0, ACTIVE = 1, FINISHED = 2 };
+  HostMol mol;
+  int state = QUEUED;
+  int slot = -1;
+  int n = 0;
+  long long nsteps = 0;
+  double t_submit = 0.0, t_done = 0.0;
+  std::vector<float> unc, vel;
+  double energy[5] = {0, 0, 0, 0, 0};
+  int status = 0;
+  long long steps = 0;
+};
+
+double now_seconds() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
 }  // namespace
 
 struct SopCtx {
@@ -104,6 +178,17 @@ struct SopCtx {
   double* h_out = nullptr;    // pinned copy of e_out
   float4* stage = nullptr;    // gather buffer of sop_download_all
   std::map<int, float> tuning;  // step-kernel time (ms) per lanes-per-bead candidate
+  Caps caps;
+  MolConst* dmol = nullptr;
+  RangeAlloc bead_alloc, bond_alloc, ang_alloc, nat_alloc;
+  std::vector<int> free_slots;  // molecule slots not in use (back = next)
+  // serving
+  bool served = false;
+  long long budget = 0;
+  std::vector<Job> jobs;
+  std::deque<int> queue;          // queued job ids in arrival order
+  std::vector<int> slot_job;      // job in each molecule slot, -1: free
+  std::vector<int> finished_new;  // finished since the last sop_serve_finished
   long long host_step = 0;    // common step of plain / batched contexts
   long long target_step = 0;  // step every molecule should reach after the queued work
   std::map<std::string, Graph> graphs;
@@ -330,14 +415,10 @@ int sync_checked(SopCtx* ctx) {
     CK(cudaMemcpyAsync(&flags, ctx->s.flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     if (!(flags & FLAG_NL_OVERFLOW)) return SOP_OK;
-    // Molecules froze at the start of the block that overflowed.  All of them
-    // share one step (plain / batched contexts), read it from molecule 0.
+    // Every molecule froze at the start of the block that overflowed; the
+    // context's clock stopped there too.
     long long done = 0;
-    int m0 = -1;
-    for (size_t m = 0; m < ctx->mc.size(); ++m)
-      if (ctx->mc[m].active) { m0 = (int)m; break; }
-    if (m0 < 0) return SOP_OK;
-    CK(cudaMemcpy(&done, ctx->s.mol_step + m0, sizeof(long long), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&done, ctx->s.sys_step, sizeof(long long), cudaMemcpyDeviceToHost));
     int rc = grow_nl(ctx);
     if (rc) return rc;
     long long target = ctx->target_step;
@@ -365,19 +446,10 @@ MolConst make_const(const sop_params& P, const HostMol& hm) {
   return c;
 }
 
-// Packs every staged molecule into the device layout.
-int commit(SopCtx* ctx) {
+// Scalar constants of the force field and the lists (DevSys fields).
+void set_constants(SopCtx* ctx) {
   const sop_params& P = ctx->P;
   DevSys& s = ctx->s;
-  int nbead = 0;
-  for (auto& m : ctx->mols) {
-    m.start = nbead;
-    nbead += m.n;
-  }
-  const int nmol = (int)ctx->mols.size();
-  if (nbead <= 0) return ctx->fail(SOP_ERR_ARG, "no beads");
-  s.nbead = nbead;
-  s.nmol = nmol;
   s.boxl = (float)P.boxl;
   s.eps_rep = (float)P.eps_rep;
   s.rep6 = P.rep6;
@@ -401,78 +473,16 @@ int commit(SopCtx* ctx) {
   s.rc_nl_rep_max = rcmax;
   s.seed_lo = (unsigned)(P.seed & 0xffffffffULL);
   s.seed_hi = (unsigned)(P.seed >> 32);
+}
 
-  // ---- host CSR rows (each pair in the rows of both beads)
-  std::vector<int2> bond_row(nbead), ang_row(nbead), nat_row(nbead);
-  std::vector<int> bond_j, ang_j, nat_j, mol_of(nbead);
-  std::vector<float> bond_r0;
-  std::vector<float4> nat_par;
-  std::vector<float2> nat_rc2;
-  std::vector<float4> x0(nbead), p0(nbead), v0(nbead);
-  long long cell_cap = 0;
-  {
-    std::vector<int> cnt_b(nbead, 0), cnt_a(nbead, 0), cnt_n(nbead, 0);
-    for (auto& m : ctx->mols) {
-      for (size_t k = 0; k < m.bi.size(); ++k) { cnt_b[m.start + m.bi[k]]++; cnt_b[m.start + m.bj[k]]++; }
-      for (size_t k = 0; k < m.ai.size(); ++k) { cnt_a[m.start + m.ai[k]]++; cnt_a[m.start + m.ak[k]]++; }
-      for (size_t k = 0; k < m.ni.size(); ++k) { cnt_n[m.start + m.ni[k]]++; cnt_n[m.start + m.nj[k]]++; }
-    }
-    int ob = 0, oa = 0, on = 0;
-    for (int i = 0; i < nbead; ++i) {
-      bond_row[i] = make_int2(ob, 0); ob += cnt_b[i];
-      ang_row[i] = make_int2(oa, 0); oa += cnt_a[i];
-      nat_row[i] = make_int2(on, 0); on += cnt_n[i];
-    }
-    bond_j.resize(ob); bond_r0.resize(ob); ang_j.resize(oa);
-    nat_j.resize(on); nat_par.resize(on); nat_rc2.resize(on);
-    auto put_b = [&](int i, int j, float r0) {
-      int e = bond_row[i].x + bond_row[i].y++;
-      bond_j[e] = j; bond_r0[e] = r0;
-    };
-    auto put_a = [&](int i, int j) { ang_j[ang_row[i].x + ang_row[i].y++] = j; };
-    auto put_n = [&](int i, int j, float r0, float ef, float ee) {
-      int e = nat_row[i].x + nat_row[i].y++;
-      nat_j[e] = j;
-      nat_par[e] = make_float4(r0, ef, ee, 0.f);
-      nat_rc2[e] = make_float2(rcut2_of(P.nl_att_fac, P.nl_att_abs, r0),
-                               rcut2_of(P.pl_att_fac, P.pl_att_abs, r0));
-    };
-    for (int mi = 0; mi < nmol; ++mi) {
-      auto& m = ctx->mols[mi];
-      const int o = m.start;
-      for (size_t k = 0; k < m.bi.size(); ++k) {
-        put_b(o + m.bi[k], o + m.bj[k], m.br0[k]);
-        put_b(o + m.bj[k], o + m.bi[k], m.br0[k]);
-      }
-      for (size_t k = 0; k < m.ai.size(); ++k) {
-        put_a(o + m.ai[k], o + m.ak[k]);
-        put_a(o + m.ak[k], o + m.ai[k]);
-      }
-      for (size_t k = 0; k < m.ni.size(); ++k) {
-        put_n(o + m.ni[k], o + m.nj[k], m.nr0[k], m.neps[k], m.nepse[k]);
-        put_n(o + m.nj[k], o + m.ni[k], m.nr0[k], m.neps[k], m.nepse[k]);
-      }
-      for (int i = 0; i < m.n; ++i) {
-        mol_of[o + i] = mi;
-        int t = m.types.empty() ? 1 : m.types[i];
-        x0[o + i] = make_float4(m.unc[3 * i], m.unc[3 * i + 1], m.unc[3 * i + 2], bits_f(t));
-        const std::vector<float>& pp = m.pos.empty() ? m.unc : m.pos;
-        p0[o + i] = make_float4(pp[3 * i], pp[3 * i + 1], pp[3 * i + 2], 0.f);
-        if (m.vel.empty()) v0[o + i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        else v0[o + i] = make_float4(m.vel[3 * i], m.vel[3 * i + 1], m.vel[3 * i + 2], 0.f);
-      }
-      cell_cap += std::max<long long>(64, 2LL * m.n);
-    }
-  }
-  s.uniform_type = 1;
-  for (auto& m : ctx->mols)
-    for (int t : m.types)
-      if (t != 1) s.uniform_type = 0;
-  ctx->mc.resize(nmol);
-  for (int mi = 0; mi < nmol; ++mi) ctx->mc[mi] = make_const(P, ctx->mols[mi]);
-
-  // ---- device allocations
-  const size_t nb = (size_t)nbead;
+// Device arrays sized by capacities: beads, molecule slots, topology entries
+// (each pair counted for both beads).  Free bead slots have mol_of = -1.
+int alloc_pools(SopCtx* ctx, const Caps& c) {
+  DevSys& s = ctx->s;
+  ctx->caps = c;
+  const size_t nb = (size_t)c.beads, nm = (size_t)c.mols;
+  s.nbead = (int)c.beads;
+  s.nmol = (int)c.mols;
   for (int b = 0; b < 2; ++b) {
     s.x[b] = ctx->dalloc<float4>(nb);
     s.p[b] = ctx->dalloc<float4>(nb);
@@ -481,37 +491,36 @@ int commit(SopCtx* ctx) {
   s.incr = ctx->dalloc<float4>(nb);
   s.f = ctx->dalloc<float4>(nb);
   s.mol_of = ctx->dalloc<int>(nb);
-  MolConst* dmol = ctx->dalloc<MolConst>(nmol);
-  s.mol = dmol;
-  s.mol_step = ctx->dalloc<long long>(nmol);
-  s.mol_status = ctx->dalloc<int>(nmol);
+  ctx->dmol = ctx->dalloc<MolConst>(nm);
+  s.mol = ctx->dmol;
+  s.mol_step = ctx->dalloc<long long>(nm);
+  s.mol_status = ctx->dalloc<int>(nm);
+  s.sys_step = ctx->dalloc<long long>(1);
   s.bond_row = ctx->dalloc<int2>(nb);
   s.ang_row = ctx->dalloc<int2>(nb);
   s.nat_row = ctx->dalloc<int2>(nb);
-  s.bond_j = ctx->dalloc<int>(bond_j.size());
-  s.bond_r0 = ctx->dalloc<float>(bond_r0.size());
-  s.ang_j = ctx->dalloc<int>(ang_j.size());
-  s.nat_j = ctx->dalloc<int>(nat_j.size());
-  s.nat_par = ctx->dalloc<float4>(nat_par.size());
-  s.nat_rc2 = ctx->dalloc<float2>(nat_rc2.size());
+  s.bond_j = ctx->dalloc<int>(c.bonds);
+  s.bond_r0 = ctx->dalloc<float>(c.bonds);
+  s.ang_j = ctx->dalloc<int>(c.angles);
+  s.nat_j = ctx->dalloc<int>(c.natives);
+  s.nat_par = ctx->dalloc<float4>(c.natives);
+  s.nat_rc2 = ctx->dalloc<float2>(c.natives);
   s.nl_att_cnt = ctx->dalloc<int>(nb);
   s.pl_att_cnt = ctx->dalloc<int>(nb);
-  s.nl_att_e = ctx->dalloc<int>(nat_j.size());
-  s.pl_att = ctx->dalloc<float4>(nat_j.size());
+  s.nl_att_e = ctx->dalloc<int>(c.natives);
+  s.pl_att = ctx->dalloc<float4>(c.natives);
   s.nl_cnt = ctx->dalloc<int>(nb);
   s.pl_cnt = ctx->dalloc<int>(nb);
   s.nl_maxrow = ctx->dalloc<int>(1);
   s.nl_j = nullptr;
   s.pl_j = nullptr;
-  {
-    int rc = alloc_nl(ctx, 64);  // regrown from the first rebuild's longest row
-    if (rc) return rc;
-  }
-  s.bbox = ctx->dalloc<unsigned>(6 * (size_t)nmol);
-  s.grid = ctx->dalloc<MolGrid>(nmol);
-  s.cell_cap = cell_cap;
-  s.cell_cnt = ctx->dalloc<int>(cell_cap);
-  s.cell_start = ctx->dalloc<int>(cell_cap + 1);
+  int rc = alloc_nl(ctx, c.stride);
+  if (rc) return rc;
+  s.bbox = ctx->dalloc<unsigned>(6 * nm);
+  s.grid = ctx->dalloc<MolGrid>(nm);
+  s.cell_cap = c.cells;
+  s.cell_cnt = ctx->dalloc<int>(c.cells);
+  s.cell_start = ctx->dalloc<int>(c.cells + 1);
   s.bead_cell = ctx->dalloc<int>(nb);
   s.bead_slot = ctx->dalloc<int>(nb);
   s.sorted = ctx->dalloc<int>(nb);
@@ -519,67 +528,223 @@ int commit(SopCtx* ctx) {
   s.flags = ctx->dalloc<int>(1);
   s.noise = nullptr;
   s.use_noise = 0;
-  ctx->w.ncell = ctx->dalloc<int>(nmol);
-  ctx->w.block_sums = ctx->dalloc<int>(scan_block_sums_needed(std::max<long long>(cell_cap, nbead)));
+  ctx->w.ncell = ctx->dalloc<int>(nm);
+  ctx->w.block_sums = ctx->dalloc<int>(scan_block_sums_needed(std::max<long long>(c.cells, nb)));
   ctx->w.cells_total = ctx->dalloc<int>(1);
-  int maxn = 0;
-  for (auto& m : ctx->mols) maxn = std::max(maxn, m.n);
-  ctx->e_part = ctx->dalloc<double>(6 * ((size_t)maxn / 256 + 2));
+  ctx->e_part = ctx->dalloc<double>(6 * ((size_t)c.max_mol_beads / 256 + 2));
   ctx->e_out = ctx->dalloc<double>(8);
-  for (void* p : ctx->allocs)
-    if (!p) return ctx->fail(SOP_ERR_ALLOC, "device allocation failed");
-  if (!s.x[0] || !s.x[1] || !s.p[0] || !s.p[1] || !s.v || !s.incr || !s.f || !s.nl_j || !s.pl_j ||
-      !s.cell_cnt || !s.cell_start || !ctx->e_part || !ctx->e_out || !ctx->w.block_sums)
+  if (!s.x[0] || !s.x[1] || !s.p[0] || !s.p[1] || !s.v || !s.incr || !s.f || !s.mol_of ||
+      !s.mol || !s.mol_step || !s.mol_status || !s.sys_step || !s.bond_row || !s.ang_row ||
+      !s.nat_row || !s.bond_j || !s.bond_r0 || !s.ang_j || !s.nat_j || !s.nat_par ||
+      !s.nat_rc2 || !s.nl_att_cnt || !s.pl_att_cnt || !s.nl_att_e || !s.pl_att || !s.nl_cnt ||
+      !s.pl_cnt || !s.nl_maxrow || !s.bbox || !s.grid || !s.cell_cnt || !s.cell_start ||
+      !s.bead_cell || !s.bead_slot || !s.sorted || !s.xs || !s.flags || !ctx->w.ncell ||
+      !ctx->w.block_sums || !ctx->w.cells_total || !ctx->e_part || !ctx->e_out)
     return ctx->fail(SOP_ERR_ALLOC, "device allocation failed");
   if (!ctx->h_out) CK(cudaMallocHost(&ctx->h_out, 8 * sizeof(double)));
-
   cudaStream_t st = ctx->stream;
-  // x_0 sits in buffer 0 (step 0 is even)
-  CK(cudaMemcpyAsync(s.x[0], x0.data(), sizeof(float4) * nb, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(s.x[1], x0.data(), sizeof(float4) * nb, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(s.p[0], p0.data(), sizeof(float4) * nb, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(s.p[1], p0.data(), sizeof(float4) * nb, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(s.v, v0.data(), sizeof(float4) * nb, cudaMemcpyHostToDevice, st));
-  CK(cudaMemsetAsync(s.incr, 0, sizeof(float4) * nb, st));
-  CK(cudaMemsetAsync(s.f, 0, sizeof(float4) * nb, st));
-  CK(cudaMemcpyAsync(s.mol_of, mol_of.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(dmol, ctx->mc.data(), sizeof(MolConst) * nmol, cudaMemcpyHostToDevice, st));
-  CK(cudaMemsetAsync(s.mol_step, 0, sizeof(long long) * nmol, st));
-  CK(cudaMemsetAsync(s.mol_status, 0, sizeof(int) * nmol, st));
-  CK(cudaMemcpyAsync(s.bond_row, bond_row.data(), sizeof(int2) * nb, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(s.ang_row, ang_row.data(), sizeof(int2) * nb, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(s.nat_row, nat_row.data(), sizeof(int2) * nb, cudaMemcpyHostToDevice, st));
-  if (!bond_j.empty()) {
-    CK(cudaMemcpyAsync(s.bond_j, bond_j.data(), sizeof(int) * bond_j.size(), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(s.bond_r0, bond_r0.data(), sizeof(float) * bond_r0.size(), cudaMemcpyHostToDevice, st));
-  }
-  if (!ang_j.empty())
-    CK(cudaMemcpyAsync(s.ang_j, ang_j.data(), sizeof(int) * ang_j.size(), cudaMemcpyHostToDevice, st));
-  if (!nat_j.empty()) {
-    CK(cudaMemcpyAsync(s.nat_j, nat_j.data(), sizeof(int) * nat_j.size(), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(s.nat_par, nat_par.data(), sizeof(float4) * nat_par.size(), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(s.nat_rc2, nat_rc2.data(), sizeof(float2) * nat_rc2.size(), cudaMemcpyHostToDevice, st));
-  }
+  CK(cudaMemsetAsync(s.mol_of, 0xff, sizeof(int) * nb, st));   // -1: free
+  CK(cudaMemsetAsync(ctx->dmol, 0, sizeof(MolConst) * nm, st));  // inactive
+  CK(cudaMemsetAsync(s.mol_step, 0, sizeof(long long) * nm, st));
+  CK(cudaMemsetAsync(s.mol_status, 0, sizeof(int) * nm, st));
+  CK(cudaMemsetAsync(s.sys_step, 0, sizeof(long long), st));
   CK(cudaMemsetAsync(s.flags, 0, sizeof(int), st));
+  CK(cudaMemsetAsync(s.nl_maxrow, 0, sizeof(int), st));
   CK(cudaMemsetAsync(s.nl_att_cnt, 0, sizeof(int) * nb, st));
   CK(cudaMemsetAsync(s.pl_att_cnt, 0, sizeof(int) * nb, st));
   CK(cudaMemsetAsync(s.nl_cnt, 0, sizeof(int) * nb, st));
   CK(cudaMemsetAsync(s.pl_cnt, 0, sizeof(int) * nb, st));
-  CK(cudaMemsetAsync(s.nl_maxrow, 0, sizeof(int), st));
+  CK(cudaMemsetAsync(s.cell_cnt, 0, sizeof(int) * (size_t)c.cells, st));
+  CK(cudaMemsetAsync(s.cell_start, 0, sizeof(int) * (size_t)(c.cells + 1), st));  // nothing binned yet
+  CK(cudaMemsetAsync(s.bond_row, 0, sizeof(int2) * nb, st));
+  CK(cudaMemsetAsync(s.ang_row, 0, sizeof(int2) * nb, st));
+  CK(cudaMemsetAsync(s.nat_row, 0, sizeof(int2) * nb, st));
+  ctx->bead_alloc.reset(c.beads);
+  ctx->bond_alloc.reset(c.bonds);
+  ctx->ang_alloc.reset(c.angles);
+  ctx->nat_alloc.reset(c.natives);
+  ctx->free_slots.clear();
+  for (long long m = c.mols - 1; m >= 0; --m) ctx->free_slots.push_back((int)m);
+  ctx->mc.assign(c.mols, MolConst{});
+  return SOP_OK;
+}
 
+// Writes molecule hm into molecule slot `slot`: bead and topology ranges from
+// the pools, rows with absolute offsets, x_0 in both coordinate buffers, its
+// lists empty, and mol_step = step0 (0: starts now; < 0: starts -step0 steps
+// into the next block sequence).  Returns SOP_ERR_CAPACITY if a pool is full.
+int install(SopCtx* ctx, int slot, HostMol& hm, long long step0) {
+  const sop_params& P = ctx->P;
+  DevSys& s = ctx->s;
+  const long long nb2 = 2LL * (long long)hm.bi.size(), na2 = 2LL * (long long)hm.ai.size(),
+                  nn2 = 2LL * (long long)hm.ni.size();
+  long long b0 = ctx->bead_alloc.alloc(hm.n);
+  if (b0 < 0) return SOP_ERR_CAPACITY;
+  long long ob = ctx->bond_alloc.alloc(nb2);
+  long long oa = ctx->ang_alloc.alloc(na2);
+  long long on = ctx->nat_alloc.alloc(nn2);
+  if (ob < 0 || oa < 0 || on < 0) {
+    ctx->bead_alloc.release(b0, hm.n);
+    if (ob >= 0) ctx->bond_alloc.release(ob, nb2);
+    if (oa >= 0) ctx->ang_alloc.release(oa, na2);
+    if (on >= 0) ctx->nat_alloc.release(on, nn2);
+    return SOP_ERR_CAPACITY;
+  }
+  hm.start = (int)b0;
+  hm.slot = slot;
+  hm.off_b = ob; hm.off_a = oa; hm.off_n = on;
+  const int n = hm.n, o = (int)b0;
+  std::vector<int2> brow(n), arow(n), nrow(n);
+  std::vector<int> cnt_b(n, 0), cnt_a(n, 0), cnt_n(n, 0);
+  for (size_t k = 0; k < hm.bi.size(); ++k) { cnt_b[hm.bi[k]]++; cnt_b[hm.bj[k]]++; }
+  for (size_t k = 0; k < hm.ai.size(); ++k) { cnt_a[hm.ai[k]]++; cnt_a[hm.ak[k]]++; }
+  for (size_t k = 0; k < hm.ni.size(); ++k) { cnt_n[hm.ni[k]]++; cnt_n[hm.nj[k]]++; }
+  {
+    int eb = (int)ob, ea = (int)oa, en = (int)on;
+    for (int i = 0; i < n; ++i) {
+      brow[i] = make_int2(eb, 0); eb += cnt_b[i];
+      arow[i] = make_int2(ea, 0); ea += cnt_a[i];
+      nrow[i] = make_int2(en, 0); en += cnt_n[i];
+    }
+  }
+  std::vector<int> bj(nb2), aj(na2), nj(nn2), molof(n, slot);
+  std::vector<float> br(nb2);
+  std::vector<float4> np(nn2);
+  std::vector<float2> nr(nn2);
+  auto put_b = [&](int i, int j, float r0) {
+    int e = brow[i].x + brow[i].y++ - (int)ob;
+    bj[e] = o + j; br[e] = r0;
+  };
+  auto put_a = [&](int i, int j) { aj[arow[i].x + arow[i].y++ - (int)oa] = o + j; };
+  auto put_n = [&](int i, int j, float r0, float ef, float ee) {
+    int e = nrow[i].x + nrow[i].y++ - (int)on;
+    nj[e] = o + j;
+    np[e] = make_float4(r0, ef, ee, 0.f);
+    nr[e] = make_float2(rcut2_of(P.nl_att_fac, P.nl_att_abs, r0),
+                        rcut2_of(P.pl_att_fac, P.pl_att_abs, r0));
+  };
+  for (size_t k = 0; k < hm.bi.size(); ++k) {
+    put_b(hm.bi[k], hm.bj[k], hm.br0[k]);
+    put_b(hm.bj[k], hm.bi[k], hm.br0[k]);
+  }
+  for (size_t k = 0; k < hm.ai.size(); ++k) {
+    put_a(hm.ai[k], hm.ak[k]);
+    put_a(hm.ak[k], hm.ai[k]);
+  }
+  for (size_t k = 0; k < hm.ni.size(); ++k) {
+    put_n(hm.ni[k], hm.nj[k], hm.nr0[k], hm.neps[k], hm.nepse[k]);
+    put_n(hm.nj[k], hm.ni[k], hm.nr0[k], hm.neps[k], hm.nepse[k]);
+  }
+  std::vector<float4> x0(n), p0(n), v0(n);
+  for (int i = 0; i < n; ++i) {
+    int t = hm.types.empty() ? 1 : hm.types[i];
+    x0[i] = make_float4(hm.unc[3 * i], hm.unc[3 * i + 1], hm.unc[3 * i + 2], bits_f(t));
+    const std::vector<float>& pp = hm.pos.empty() ? hm.unc : hm.pos;
+    p0[i] = make_float4(pp[3 * i], pp[3 * i + 1], pp[3 * i + 2], 0.f);
+    v0[i] = hm.vel.empty() ? make_float4(0.f, 0.f, 0.f, 0.f)
+                           : make_float4(hm.vel[3 * i], hm.vel[3 * i + 1], hm.vel[3 * i + 2], 0.f);
+  }
+  MolConst mcst = make_const(P, hm);
+  ctx->mc[slot] = mcst;
+  cudaStream_t st = ctx->stream;
+  const size_t f4 = sizeof(float4) * n;
+  for (int b = 0; b < 2; ++b) {
+    CK(cudaMemcpyAsync(s.x[b] + o, x0.data(), f4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s.p[b] + o, p0.data(), f4, cudaMemcpyHostToDevice, st));
+  }
+  CK(cudaMemcpyAsync(s.v + o, v0.data(), f4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(s.incr + o, 0, f4, st));
+  CK(cudaMemsetAsync(s.f + o, 0, f4, st));
+  CK(cudaMemcpyAsync(s.bond_row + o, brow.data(), sizeof(int2) * n, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(s.ang_row + o, arow.data(), sizeof(int2) * n, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(s.nat_row + o, nrow.data(), sizeof(int2) * n, cudaMemcpyHostToDevice, st));
+  if (nb2) {
+    CK(cudaMemcpyAsync(s.bond_j + ob, bj.data(), sizeof(int) * nb2, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s.bond_r0 + ob, br.data(), sizeof(float) * nb2, cudaMemcpyHostToDevice, st));
+  }
+  if (na2) CK(cudaMemcpyAsync(s.ang_j + oa, aj.data(), sizeof(int) * na2, cudaMemcpyHostToDevice, st));
+  if (nn2) {
+    CK(cudaMemcpyAsync(s.nat_j + on, nj.data(), sizeof(int) * nn2, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s.nat_par + on, np.data(), sizeof(float4) * nn2, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s.nat_rc2 + on, nr.data(), sizeof(float2) * nn2, cudaMemcpyHostToDevice, st));
+  }
+  CK(cudaMemsetAsync(s.nl_cnt + o, 0, sizeof(int) * n, st));
+  CK(cudaMemsetAsync(s.pl_cnt + o, 0, sizeof(int) * n, st));
+  CK(cudaMemsetAsync(s.nl_att_cnt + o, 0, sizeof(int) * n, st));
+  CK(cudaMemsetAsync(s.pl_att_cnt + o, 0, sizeof(int) * n, st));
+  CK(cudaStreamSynchronize(st));  // the host vectors above go out of scope
+  CK(cudaMemcpy(s.mol_step + slot, &step0, sizeof(long long), cudaMemcpyHostToDevice));
+  CK(cudaMemset(s.mol_status + slot, 0, sizeof(int)));
+  CK(cudaMemcpy(s.mol_of + o, molof.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->dmol + slot, &mcst, sizeof(MolConst), cudaMemcpyHostToDevice));
+  return SOP_OK;
+}
+
+// Frees molecule slot `slot`: inactive on the device, its beads unowned,
+// its pool ranges returned.  The stream must be idle.
+int uninstall(SopCtx* ctx, int slot) {
+  HostMol& hm = ctx->mols[slot];
+  if (hm.start < 0) return SOP_OK;
+  MolConst off{};
+  CK(cudaMemcpy(ctx->dmol + slot, &off, sizeof(MolConst), cudaMemcpyHostToDevice));
+  CK(cudaMemset(ctx->s.mol_of + hm.start, 0xff, sizeof(int) * (size_t)hm.n));
+  ctx->bead_alloc.release(hm.start, hm.n);
+  ctx->bond_alloc.release(hm.off_b, 2LL * (long long)hm.bi.size());
+  ctx->ang_alloc.release(hm.off_a, 2LL * (long long)hm.ai.size());
+  ctx->nat_alloc.release(hm.off_n, 2LL * (long long)hm.ni.size());
+  ctx->mc[slot] = MolConst{};
+  hm.start = -1;
+  ctx->free_slots.push_back(slot);
+  return SOP_OK;
+}
+
+// Set-up after installing molecules at step 0: lists from x_0, f_0 and the
+// look-ahead (sop.cu:142-186), and the lanes-per-bead choice.
+int setup_step0(SopCtx* ctx) {
   const int fixed_g = lanes_for(ctx);
   ctx->G = fixed_g ? fixed_g : 8;
-  // set-up of underdamped_ctrl: lists from x_0, then f_0 and the look-ahead
   int rc = nl_rebuild_checked(ctx, 0);
   if (rc) return rc;
-  launch_pl_rebuild(s, 0, st);
+  launch_pl_rebuild(ctx->s, 0, ctx->stream);
   force_eval_async(ctx);
   CK(cudaGetLastError());
   if (!fixed_g) {
     rc = autotune_lanes(ctx);
     if (rc) return rc;
   }
-  CK(cudaStreamSynchronize(st));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SOP_OK;
+}
+
+// Packs every staged molecule into exactly sized pools (plain and batched
+// contexts): molecule id = slot, all at step 0.
+int commit(SopCtx* ctx) {
+  set_constants(ctx);
+  Caps c;
+  for (auto& m : ctx->mols) {
+    c.beads += m.n;
+    c.bonds += 2LL * (long long)m.bi.size();
+    c.angles += 2LL * (long long)m.ai.size();
+    c.natives += 2LL * (long long)m.ni.size();
+    c.cells += std::max<long long>(64, 2LL * m.n);
+    c.max_mol_beads = std::max<long long>(c.max_mol_beads, m.n);
+  }
+  c.mols = (long long)ctx->mols.size();
+  if (c.beads <= 0) return ctx->fail(SOP_ERR_ARG, "no beads");
+  c.stride = 64;  // regrown from the first rebuild's longest row
+  int rc = alloc_pools(ctx, c);
+  if (rc) return rc;
+  ctx->s.uniform_type = 1;
+  for (auto& m : ctx->mols)
+    for (int t : m.types)
+      if (t != 1) ctx->s.uniform_type = 0;
+  for (int k = 0; k < (int)ctx->mols.size(); ++k) {
+    ctx->free_slots.pop_back();  // slots handed out in id order
+    rc = install(ctx, k, ctx->mols[k], 0);
+    if (rc) return ctx->fail(rc, "pool sizing error");
+  }
+  rc = setup_step0(ctx);
+  if (rc) return rc;
   ctx->host_step = 0;
   ctx->target_step = 0;
   ctx->committed = true;
@@ -669,13 +834,16 @@ int sop_ctx_destroy(void* p) {
   return SOP_OK;
 }
 
-int sop_add_molecule(void* p, const sop_molecule* m, int* mol_id) {
-  if (!p || !m) return SOP_ERR_ARG;
-  SopCtx* ctx = C(p);
-  if (ctx->committed) return ctx->fail(SOP_ERR_ARG, "context already committed");
+}  // extern "C"
+
+// Validates a molecule description and copies it to host storage.
+static int make_hostmol(SopCtx* ctx, const sop_molecule* m, HostMol& h) {
   if (m->nbead <= 0 || !m->unc_pos) return ctx->fail(SOP_ERR_ARG, "molecule needs beads and coordinates");
   if (m->nbnd < 0 || m->nang < 0 || m->nnat < 0) return ctx->fail(SOP_ERR_ARG, "negative counts");
-  HostMol h;
+  if ((m->nbnd && (!m->bond_i || !m->bond_j || !m->bond_r0)) || (m->nang && (!m->ang_i || !m->ang_k)) ||
+      (m->nnat && (!m->nat_i || !m->nat_j || !m->nat_r0)))
+    return ctx->fail(SOP_ERR_ARG, "missing topology arrays");
+  h = HostMol();
   h.n = m->nbead;
   auto in = [&](int v) { return v >= 0 && v < m->nbead; };
   for (int k = 0; k < m->nbnd; ++k)
@@ -709,8 +877,233 @@ int sop_add_molecule(void* p, const sop_molecule* m, int* mol_id) {
   h.T = m->T;
   h.traj = m->traj;
   h.nsteps = m->nsteps;
+  return SOP_OK;
+}
+
+// ------------------------------------------------------------- serving
+static int retire(SopCtx* ctx, int slot, const std::vector<long long>& steps,
+                  const std::vector<int>& status) {
+  Job& jb = ctx->jobs[ctx->slot_job[slot]];
+  HostMol& hm = ctx->mols[slot];
+  const long long st = std::max<long long>(steps[slot], 0);
+  const int cur = (int)(st & 1);
+  jb.unc.resize(3 * (size_t)hm.n);
+  jb.vel.resize(3 * (size_t)hm.n);
+  int rc = copy3(ctx, jb.unc.data(), ctx->s.x[cur] + hm.start, hm.n);
+  if (rc) return rc;
+  rc = copy3(ctx, jb.vel.data(), ctx->s.v + hm.start, hm.n);
+  if (rc) return rc;
+  launch_energy(ctx->s, hm.start, hm.n, slot, ctx->e_part, ctx->e_out,
+                0.5 * ctx->P.k_bnd * ctx->P.R0 * ctx->P.R0, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(ctx->h_out, ctx->e_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (int t = 0; t < 4; ++t) jb.energy[t] = ctx->h_out[t];
+  jb.energy[4] = jb.energy[0] + jb.energy[1] + jb.energy[2] + jb.energy[3];
+  jb.status = status[slot] | (st >= jb.nsteps ? SOP_MOL_DONE : 0);
+  jb.steps = st;
+  jb.t_done = now_seconds();
+  jb.state = Job::FINISHED;
+  ctx->finished_new.push_back(ctx->slot_job[slot]);
+  rc = uninstall(ctx, slot);
+  if (rc) return rc;
+  ctx->slot_job[slot] = -1;
+  hm = HostMol();
+  return SOP_OK;
+}
+
+// One round: wait, retire, admit, queue nnlup steps.
+static int serve_round(SopCtx* ctx) {
+  int rc = sync_checked(ctx);
+  if (rc) return rc;
+  const int nm = (int)ctx->caps.mols;
+  std::vector<long long> steps(nm);
+  std::vector<int> status(nm);
+  CK(cudaMemcpy(steps.data(), ctx->s.mol_step, sizeof(long long) * nm, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(status.data(), ctx->s.mol_status, sizeof(int) * nm, cudaMemcpyDeviceToHost));
+  for (int slot = 0; slot < nm; ++slot) {
+    const int id = ctx->slot_job[slot];
+    if (id < 0) continue;
+    if (status[slot] != 0 || steps[slot] >= ctx->jobs[id].nsteps) {
+      rc = retire(ctx, slot, steps, status);
+      if (rc) return rc;
+    }
+  }
+  // admission in arrival order; a job that does not fit yet lets the next
+  // few (smaller) ones try
+  int looked = 0;
+  for (auto it = ctx->queue.begin(); it != ctx->queue.end() && looked < 64 && !ctx->free_slots.empty();) {
+    Job& jb = ctx->jobs[*it];
+    const int slot = ctx->free_slots.back();
+    ctx->mols[slot] = jb.mol;
+    for (int t : jb.mol.types)
+      if (t != 1 && ctx->s.uniform_type) {
+        ctx->s.uniform_type = 0;
+        ctx->drop_graphs();  // kernel arguments changed
+      }
+    rc = install(ctx, slot, ctx->mols[slot], -(long long)ctx->P.nnlup);
+    if (rc == SOP_ERR_CAPACITY) {
+      ctx->mols[slot] = HostMol();
+      ++it;
+      ++looked;
+      continue;
+    }
+    if (rc) return rc;
+    ctx->free_slots.pop_back();
+    ctx->slot_job[slot] = *it;
+    jb.slot = slot;
+    jb.state = Job::ACTIVE;
+    jb.mol = HostMol();
+    it = ctx->queue.erase(it);
+  }
+  bool any = false;
+  for (int id : ctx->slot_job) any |= id >= 0;
+  if (any) return step_async(ctx, ctx->P.nnlup);
+  return SOP_OK;
+}
+
+extern "C" {
+
+int sop_add_molecule(void* p, const sop_molecule* m, int* mol_id) {
+  if (!p || !m) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (ctx->committed) return ctx->fail(SOP_ERR_ARG, "context already committed");
+  HostMol h;
+  int rc = make_hostmol(ctx, m, h);
+  if (rc) return rc;
   ctx->mols.push_back(std::move(h));
   if (mol_id) *mol_id = (int)ctx->mols.size() - 1;
+  return SOP_OK;
+}
+
+int sop_serve_create(const sop_params* p, long long budget_bytes, long long max_job_beads,
+                     void** out) {
+  if (!p || !out || budget_bytes <= 0 || max_job_beads <= 0) return SOP_ERR_ARG;
+  if (p->nnlup <= 0) {
+    g_lib_error = "serving needs a neighbour-list cadence (nnlup > 0)";
+    return SOP_ERR_ARG;
+  }
+  int rc = sop_ctx_create(p, out);
+  if (rc) return rc;
+  SopCtx* ctx = C(*out);
+  ctx->served = true;
+  ctx->budget = budget_bytes;
+  // graph blocks must tile the neighbour-list period
+  int P = graph_steps(ctx);
+  if (ctx->P.nnlup % P) ctx->P.graph_steps = std::gcd(P, ctx->P.nnlup);
+  set_constants(ctx);
+  // list rows: about 1.3 x the neighbours of a bead in a dense (2.8e-3 / A^3) globule
+  const double rc_nl = ctx->s.rc_nl_rep_max;
+  long long stride = (long long)(1.3 * 2.8e-3 * 4.18879 * rc_nl * rc_nl * rc_nl) + 32;
+  stride = std::max<long long>(64, (stride + 31) / 32 * 32);
+  // bytes per bead slot: state (8 float4), counters and cell data (10 ints),
+  // rows (3 int2), topology (2 bond, 2 angle, 8 native entries) and list rows
+  const long long per_bead = 128 + 40 + 24 + 16 + 8 + 8 * 48 + 8 * stride;
+  Caps c;
+  c.beads = std::max<long long>(max_job_beads, budget_bytes / per_bead);
+  c.mols = std::max<long long>(64, c.beads / 50);
+  c.bonds = 2 * c.beads;
+  c.angles = 2 * c.beads;
+  c.natives = 8 * c.beads;
+  c.cells = 2 * c.beads + 64 * c.mols;
+  c.max_mol_beads = max_job_beads;
+  c.stride = stride;
+  rc = alloc_pools(ctx, c);
+  if (rc) {
+    std::string msg = ctx->err;
+    sop_ctx_destroy(*out);
+    *out = nullptr;
+    g_lib_error = msg;
+    return rc;
+  }
+  ctx->s.uniform_type = 1;
+  ctx->mols.assign(c.mols, HostMol());
+  ctx->slot_job.assign(c.mols, -1);
+  const int fixed_g = lanes_for(ctx);
+  ctx->G = fixed_g ? fixed_g : 4;
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->committed = true;
+  ctx->host_step = 0;
+  ctx->target_step = 0;
+  return SOP_OK;
+}
+
+int sop_serve_submit(void* p, const sop_molecule* m, int* job) {
+  if (!p || !m) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (!ctx->served) return ctx->fail(SOP_ERR_ARG, "not a served context");
+  if (m->nsteps < 0) return ctx->fail(SOP_ERR_ARG, "a job needs a step budget (nsteps >= 0)");
+  if (m->nbead > ctx->caps.max_mol_beads)
+    return ctx->fail(SOP_ERR_BUDGET, "job larger than the context's max_job_beads");
+  Job jb;
+  int rc = make_hostmol(ctx, m, jb.mol);
+  if (rc) return rc;
+  jb.n = m->nbead;
+  jb.nsteps = m->nsteps;
+  jb.t_submit = now_seconds();
+  ctx->jobs.push_back(std::move(jb));
+  const int id = (int)ctx->jobs.size() - 1;
+  ctx->queue.push_back(id);
+  if (job) *job = id;
+  return SOP_OK;
+}
+
+int sop_serve_advance(void* p, int rounds) {
+  if (!p || rounds < 0) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (!ctx->served) return ctx->fail(SOP_ERR_ARG, "not a served context");
+  for (int r = 0; r < rounds; ++r) {
+    int rc = serve_round(ctx);
+    if (rc) return rc;
+  }
+  return SOP_OK;
+}
+
+int sop_serve_finished(void* p, int cap, int* jobs, int* count) {
+  if (!p || cap < 0) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  int k = 0;
+  while (k < cap && !ctx->finished_new.empty()) {
+    if (jobs) jobs[k] = ctx->finished_new.front();
+    ctx->finished_new.erase(ctx->finished_new.begin());
+    ++k;
+  }
+  if (count) *count = k;
+  return SOP_OK;
+}
+
+int sop_serve_result(void* p, int job, float* unc_pos, float* vel, double* energy, int* status,
+                     long long* steps, double* latency_s) {
+  if (!p) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (job < 0 || job >= (int)ctx->jobs.size()) return ctx->fail(SOP_ERR_NOT_FOUND, "unknown job");
+  const Job& jb = ctx->jobs[job];
+  if (jb.state != Job::FINISHED) return ctx->fail(SOP_ERR_ARG, "job not finished");
+  if (unc_pos) std::memcpy(unc_pos, jb.unc.data(), sizeof(float) * jb.unc.size());
+  if (vel) std::memcpy(vel, jb.vel.data(), sizeof(float) * jb.vel.size());
+  if (energy) std::memcpy(energy, jb.energy, sizeof(jb.energy));
+  if (status) *status = jb.status;
+  if (steps) *steps = jb.steps;
+  if (latency_s) *latency_s = jb.t_done - jb.t_submit;
+  return SOP_OK;
+}
+
+int sop_serve_stats(void* p, long long* out) {
+  if (!p || !out) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  long long active = 0, beads = 0, done = 0;
+  for (const Job& jb : ctx->jobs) {
+    if (jb.state == Job::ACTIVE) { ++active; beads += jb.n; }
+    if (jb.state == Job::FINISHED) ++done;
+  }
+  out[0] = (long long)ctx->queue.size();
+  out[1] = active;
+  out[2] = done;
+  out[3] = beads;
+  out[4] = ctx->caps.beads;
+  out[5] = ctx->bytes;
+  out[6] = ctx->budget;
+  out[7] = ctx->host_step;
   return SOP_OK;
 }
 

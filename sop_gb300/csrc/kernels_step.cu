@@ -37,12 +37,16 @@ __global__ void __launch_bounds__(256) k_step(DevSys s, int koff) {
   const int nbinned = s.cell_start[s.cell_cap];
   int i = -1;
   long long n = 0;
-  if (k < nbinned && !(*s.flags & FLAG_NL_OVERFLOW)) {
-    const int b = s.sorted[k];
-    const int m = s.mol_of[b];
-    const MolConst& mc = s.mol[m];
-    n = s.mol_step[m] + (STEP ? 1 : 0) + koff;
-    if (mc.active && s.mol_status[m] == 0 && !(STEP && mc.nsteps >= 0 && n > mc.nsteps)) i = b;
+  const int b1 = (k < nbinned && !(*s.flags & FLAG_NL_OVERFLOW)) ? s.sorted[k] : -1;
+  // the cell order is from the last rebuild: a slot freed since then has no molecule
+  const int m1 = b1 >= 0 ? s.mol_of[b1] : -1;
+  if (m1 >= 0) {
+    const MolConst& mc = s.mol[m1];
+    n = s.mol_step[m1] + (STEP ? 1 : 0) + koff;
+    // n < 0: a molecule admitted to a running context whose step 0 comes later
+    // in this block; n > nsteps: finished
+    if (mc.active && s.mol_status[m1] == 0 && n >= 0 && !(STEP && mc.nsteps >= 0 && n > mc.nsteps))
+      i = b1;
   }
   // Forces are summed in a fixed order whatever G is: entry e of a row
   // accumulates into virtual lane e % kV (in increasing e), and the kV partial
@@ -219,7 +223,8 @@ __global__ void __launch_bounds__(256) k_step(DevSys s, int koff) {
   s.f[b] = make_float4(fxx, fyy, fzz, 0.f);
   float4 vi = s.v[b];
   float4 inc = s.incr[b];
-  if (STEP && !mc.t_zero) {
+  // step 0 is the initial force evaluation (sop.cu:180-186): velocities stay
+  if (STEP && nb > 0 && !mc.t_zero) {
     vi = make_float4(mc.a3 * inc.x + mc.a4 * fxx, mc.a3 * inc.y + mc.a4 * fyy,
                      mc.a3 * inc.z + mc.a4 * fzz, 0.f);
     s.v[b] = vi;
@@ -240,8 +245,9 @@ __global__ void __launch_bounds__(256) k_step(DevSys s, int koff) {
 // everything until the host regrows the list and re-runs the block.
 __global__ void k_advance(DevSys s, int steps) {
   int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= s.nmol) return;
   if (*s.flags & FLAG_NL_OVERFLOW) return;
+  if (m == 0) *s.sys_step += steps;  // the context's clock (blocks completed)
+  if (m >= s.nmol) return;
   const MolConst mc = s.mol[m];
   if (!mc.active || s.mol_status[m] != 0) return;
   long long st = s.mol_step[m] + steps;

@@ -76,7 +76,8 @@ struct DevSys {
   float4* f;
   int* mol_of;
   const MolConst* mol;
-  long long* mol_step;          // last completed step of each molecule
+  long long* mol_step;          // last completed step of each molecule (< 0: starts later)
+  long long* sys_step;          // steps the context has completed (its clock)
   int* mol_status;              // SOP_MOL_* bits
 
   int2* bond_row; int* bond_j; float* bond_r0;

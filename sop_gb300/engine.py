@@ -107,6 +107,13 @@ def lib() -> ctypes.CDLL:
             "sop_tuning": (I, [V, ctypes.POINTER(I), V]),
             "sop_stream": (I, [V, ctypes.POINTER(V)]),
             "sop_last_error": (ctypes.c_char_p, [V]),
+            "sop_serve_create": (I, [ctypes.POINTER(Params), LL, LL, ctypes.POINTER(V)]),
+            "sop_serve_submit": (I, [V, ctypes.POINTER(MoleculeDesc), ctypes.POINTER(I)]),
+            "sop_serve_advance": (I, [V, I]),
+            "sop_serve_finished": (I, [V, I, V, ctypes.POINTER(I)]),
+            "sop_serve_result": (I, [V, I, V, V, V, ctypes.POINTER(I), PLL,
+                                     ctypes.POINTER(ctypes.c_double)]),
+            "sop_serve_stats": (I, [V, V]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -300,6 +307,101 @@ class Engine:
         s = ctypes.c_void_p()
         self._check(lib().sop_stream(self.h, ctypes.byref(s)), self.h)
         return s.value or 0
+
+
+def _describe(mol: Molecule, xyz, T, traj, nsteps, keep: list, vel=None, eps_energy=None):
+    x = np.ascontiguousarray(mol.xyz if xyz is None else xyz, np.float32)
+    arrs = dict(bi=mol.bond_i, bj=mol.bond_j, br=mol.bond_r0, ai=mol.ang_i, ak=mol.ang_k,
+                ni=mol.nat_i, nj=mol.nat_j, nr=mol.nat_r0, ne=mol.nat_eps, ty=mol.types)
+    a = {k: np.ascontiguousarray(v, np.float32 if k in ("br", "nr", "ne") else np.int32)
+         for k, v in arrs.items()}
+    v = None if vel is None else np.ascontiguousarray(vel, np.float32)
+    ee = None if eps_energy is None else np.ascontiguousarray(eps_energy, np.float32)
+    keep += [x, v, ee, *a.values()]
+    return MoleculeDesc(mol.n, len(a["bi"]), _p(a["bi"]), _p(a["bj"]), _p(a["br"]),
+                        len(a["ai"]), _p(a["ai"]), _p(a["ak"]), len(a["ni"]), _p(a["ni"]),
+                        _p(a["nj"]), _p(a["nr"]), _p(a["ne"]), _p(ee), _p(a["ty"]), _p(x),
+                        None, _p(v), float(T), int(traj), int(nsteps))
+
+
+class Server:
+    """A served context (include/sop_gpu.h, sop_serve_*): jobs submitted while
+    others run, admitted by HBM budget at neighbour-list boundaries."""
+
+    def __init__(self, params: Params, budget_bytes: int, max_job_beads: int):
+        self.params = params
+        h = ctypes.c_void_p()
+        rc = lib().sop_serve_create(ctypes.byref(params), int(budget_bytes), int(max_job_beads),
+                                    ctypes.byref(h))
+        if rc != SOP_OK:
+            raise SopError(rc, (lib().sop_last_error(None) or b"").decode())
+        self.h = h
+        self.sizes = {}
+
+    def _check(self, rc):
+        if rc != SOP_OK:
+            raise SopError(rc, (lib().sop_last_error(self.h) or b"").decode())
+
+    def submit(self, mol: Molecule, xyz=None, nsteps: int = 1000, T: float = 0.6,
+               traj: int = 0) -> int:
+        keep = []
+        d = _describe(mol, xyz, T, traj, nsteps, keep)
+        job = ctypes.c_int()
+        self._check(lib().sop_serve_submit(self.h, ctypes.byref(d), ctypes.byref(job)))
+        self.sizes[job.value] = mol.n
+        return job.value
+
+    def advance(self, rounds: int = 1) -> None:
+        self._check(lib().sop_serve_advance(self.h, int(rounds)))
+
+    def finished(self) -> list[int]:
+        out = np.zeros(4096, np.int32)
+        cnt = ctypes.c_int()
+        self._check(lib().sop_serve_finished(self.h, len(out), _p(out), ctypes.byref(cnt)))
+        return out[:cnt.value].tolist()
+
+    def result(self, job: int) -> dict:
+        n = self.sizes[job]
+        unc = np.empty((n, 3), np.float32)
+        vel = np.empty((n, 3), np.float32)
+        en = np.zeros(5, np.float64)
+        st, steps, lat = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_double()
+        self._check(lib().sop_serve_result(self.h, job, _p(unc), _p(vel), _p(en), ctypes.byref(st),
+                                           ctypes.byref(steps), ctypes.byref(lat)))
+        return {"unc_pos": unc, "vel": vel, "energy": en, "status": st.value,
+                "steps": steps.value, "latency_s": lat.value}
+
+    def stats(self) -> dict:
+        o = np.zeros(8, np.int64)
+        self._check(lib().sop_serve_stats(self.h, _p(o)))
+        keys = ("queued", "active", "finished", "active_beads", "bead_capacity", "device_bytes",
+                "budget", "clock")
+        return dict(zip(keys, (int(v) for v in o)))
+
+    def run_until_idle(self, max_rounds: int = 100000) -> None:
+        for _ in range(max_rounds):
+            s = self.stats()
+            if s["queued"] == 0 and s["active"] == 0:
+                return
+            self.advance(1)
+        raise RuntimeError("server did not drain")
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().sop_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def plain(mol: Molecule, xyz=None, params: Params | None = None, T: float = 0.6, traj: int = 0,
