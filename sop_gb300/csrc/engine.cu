@@ -703,9 +703,11 @@ int uninstall(SopCtx* ctx, int slot) {
 int setup_step0(SopCtx* ctx) {
   const int fixed_g = lanes_for(ctx);
   ctx->G = fixed_g ? fixed_g : 8;
-  int rc = nl_rebuild_checked(ctx, 0);
+  // block offset -1: these rebuilds precede the force evaluation of the
+  // current step itself (x_0 sits in both coordinate buffers)
+  int rc = nl_rebuild_checked(ctx, -1);
   if (rc) return rc;
-  launch_pl_rebuild(ctx->s, 0, ctx->stream);
+  launch_pl_rebuild(ctx->s, -1, ctx->stream);
   force_eval_async(ctx);
   CK(cudaGetLastError());
   if (!fixed_g) {
@@ -1136,23 +1138,28 @@ int sop_upload_state(void* p, int mol, const float* pos, const float* unc_pos, c
   std::vector<float4> buf(hm.n);
   std::vector<float4> old(hm.n);
   CK(cudaMemcpy(old.data(), ctx->s.x[cur] + hm.start, sizeof(float4) * hm.n, cudaMemcpyDeviceToHost));
+  // the new state goes to both coordinate buffers: the lists are rebuilt from
+  // it at block offset -1 (before this step's force evaluation), and the
+  // force evaluation reads buffer step & 1
   if (unc_pos) {
     for (int i = 0; i < hm.n; ++i)
       buf[i] = make_float4(unc_pos[3 * i], unc_pos[3 * i + 1], unc_pos[3 * i + 2], old[i].w);
-    CK(cudaMemcpy(ctx->s.x[cur] + hm.start, buf.data(), sizeof(float4) * hm.n, cudaMemcpyHostToDevice));
+    for (int b = 0; b < 2; ++b)
+      CK(cudaMemcpy(ctx->s.x[b] + hm.start, buf.data(), sizeof(float4) * hm.n, cudaMemcpyHostToDevice));
   }
   const float* pp = pos ? pos : unc_pos;
   if (pp) {
     for (int i = 0; i < hm.n; ++i) buf[i] = make_float4(pp[3 * i], pp[3 * i + 1], pp[3 * i + 2], 0.f);
-    CK(cudaMemcpy(ctx->s.p[cur] + hm.start, buf.data(), sizeof(float4) * hm.n, cudaMemcpyHostToDevice));
+    for (int b = 0; b < 2; ++b)
+      CK(cudaMemcpy(ctx->s.p[b] + hm.start, buf.data(), sizeof(float4) * hm.n, cudaMemcpyHostToDevice));
   }
   if (vel) {
     for (int i = 0; i < hm.n; ++i) buf[i] = make_float4(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], 0.f);
     CK(cudaMemcpy(ctx->s.v + hm.start, buf.data(), sizeof(float4) * hm.n, cudaMemcpyHostToDevice));
   }
-  rc = nl_rebuild_checked(ctx, 0);
+  rc = nl_rebuild_checked(ctx, -1);
   if (rc) return rc;
-  launch_pl_rebuild(ctx->s, 0, ctx->stream);
+  launch_pl_rebuild(ctx->s, -1, ctx->stream);
   force_eval_async(ctx);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));

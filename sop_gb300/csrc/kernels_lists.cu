@@ -114,8 +114,15 @@ __global__ void k_bbox_reset(DevSys s) {
   b[3] = b[4] = b[5] = f2ord(-INFINITY);
 }
 
-__device__ __forceinline__ bool mol_listed(const DevSys& s, int m) {
-  return m >= 0 && s.mol[m].active && s.mol_status[m] == 0;
+// Molecules whose lists a rebuild at block offset koff refreshes: running,
+// healthy, and with the step this rebuild precedes (mol_step + koff + 1)
+// still within the step budget -- a molecule that has finished keeps the
+// lists of its last step, as the reference's loop ends there.
+__device__ __forceinline__ bool mol_listed(const DevSys& s, int m, int koff) {
+  if (m < 0) return false;
+  const MolConst& mc = s.mol[m];
+  return mc.active && s.mol_status[m] == 0 &&
+         !(mc.nsteps >= 0 && s.mol_step[m] + koff >= mc.nsteps);
 }
 
 // Coordinates at step mol_step + koff (the positions the rebuild uses).
@@ -126,7 +133,7 @@ __device__ __forceinline__ const float4* xbuf(const DevSys& s, int m, int koff) 
 __global__ void k_bbox(DevSys s, int koff) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int m = (i < s.nbead) ? s.mol_of[i] : -1;
-  bool ok = mol_listed(s, m);
+  bool ok = mol_listed(s, m, koff);
   unsigned act = __ballot_sync(0xffffffffu, ok);
   if (!ok) return;
   float4 x = xbuf(s, m, koff)[i];
@@ -149,12 +156,12 @@ __global__ void k_bbox(DevSys s, int koff) {
 }
 
 // One thread per molecule: cell grid of its neighbour-list build.
-__global__ void k_grid(DevSys s, int* __restrict__ ncell) {
+__global__ void k_grid(DevSys s, int* __restrict__ ncell, int koff) {
   int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= s.nmol) return;
   MolGrid g = {};
   int n = s.mol[m].n;
-  if (!mol_listed(s, m) || n <= 0) {
+  if (!mol_listed(s, m, koff) || n <= 0) {
     g.ncell = 0;
     s.grid[m] = g;
     ncell[m] = 0;
@@ -235,9 +242,8 @@ __global__ void k_assign(DevSys s, int koff) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= s.nbead) return;
   int m = s.mol_of[i];
-  if (!mol_listed(s, m)) {
+  if (!mol_listed(s, m, koff)) {  // not binned; its lists stay as they are
     s.bead_cell[i] = -1;
-    s.nl_att_cnt[i] = 0;
     return;
   }
   const float4* X = xbuf(s, m, koff);
@@ -422,10 +428,7 @@ __global__ void __launch_bounds__(256) k_pl(DevSys s, int koff) {
   if (*s.flags & FLAG_NL_OVERFLOW) return;
   const int i = s.sorted[kk];
   const int m = s.mol_of[i];
-  if (!mol_listed(s, m)) {
-    if (lane == 0) { s.pl_cnt[i] = 0; s.pl_att_cnt[i] = 0; }
-    return;
-  }
+  if (!mol_listed(s, m, koff)) return;  // finished or stopped: keeps the lists of its last step
   const float4* X = xbuf(s, m, koff);
   const float4 xi = X[i];
   const int ti = type_of(xi);
@@ -516,7 +519,7 @@ void launch_nl_rebuild(const DevSys& s, const NLScratch& w, int koff, cudaStream
   const int T = 256;
   k_bbox_reset<<<cdiv(s.nmol, T), T, 0, st>>>(s);
   k_bbox<<<cdiv(s.nbead, T), T, 0, st>>>(s, koff);
-  k_grid<<<cdiv(s.nmol, T), T, 0, st>>>(s, w.ncell);
+  k_grid<<<cdiv(s.nmol, T), T, 0, st>>>(s, w.ncell, koff);
   k_grid_base<<<1, 1024, 0, st>>>(s, w.ncell, w.cells_total);
   cudaMemsetAsync(s.cell_cnt, 0, sizeof(int) * (size_t)s.cell_cap, st);
   k_assign<<<cdiv(s.nbead, T), T, 0, st>>>(s, koff);

@@ -51,7 +51,7 @@ def test_mix_equals_alone_with_queueing_and_slot_reuse():
     p = params()
     # a budget that holds only part of the stream at once: jobs queue and
     # later ones reuse the slots of earlier ones
-    with engine.Server(p, budget_bytes=64 << 20, max_job_beads=1500) as srv:
+    with engine.Server(p, budget_bytes=12 << 20, max_job_beads=1500) as srv:
         cap = srv.stats()["bead_capacity"]
         assert cap < sum(j[0] for j in JOBS)
         ids = [srv.submit(mol_of(n, s), start_xyz(mol_of(n, s), ext), nsteps=st, T=T, traj=100 + k)
