@@ -262,6 +262,44 @@ int sop_serve_result(void* ctx, int job, float* unc_pos, float* vel, double* ene
  * device bytes held; budget; the context's step clock. */
 int sop_serve_stats(void* ctx, long long* out);
 
+/*
+ * Energy without allocation.  No counterpart in the reference: an extension
+ * for callers that may not allocate device memory -- a host application whose
+ * own memory manager owns every device byte, a loop that must not stall on the
+ * implicit synchronisation cudaMalloc / cudaFree can bring, or an embedding
+ * whose framework forbids allocations outside its pool.  The caller owns every
+ * buffer below (device memory) and the output; the call only launches kernels
+ * on `stream` (a cudaStream_t, NULL for the default stream) and returns
+ * without waiting.
+ *
+ * Lists are in the reference's layout (energy.cu:194-442), 0-based bead
+ * pairs: bonds with native lengths, i,i+2 angle pairs, native pairs with r0
+ * and epsilon (NULL: 1.0), non-native pairs.  terms receives 5 doubles as
+ * sop_energy: e_bnd, e_ang_ss, e_vdw_rr_att, e_vdw_rr_rep, rna_etot.
+ *
+ * Limit: at most SOP_ENERGY_NOALLOC_MAX_ITEMS list entries in total (bonds +
+ * angles + native + non-native pairs); larger inputs fail with
+ * SOP_ERR_CAPACITY.  The per-block partial sums live in one fixed 128 KiB
+ * device array that every GPU loading the library holds until the process
+ * exits.  The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress) with the device current; make that first call before
+ * any stream capture.  Every call shares the array and overwrites the part it
+ * uses, so calls that overlap on the GPU (different streams, or different host
+ * threads on one device) race; serialise them.
+ */
+#define SOP_ENERGY_NOALLOC_MAX_ITEMS 4194304LL
+typedef struct sop_energy_lists {
+  int nbead;  const float* unc_pos;                 /* 3*nbead floats */
+  const int* types;                                 /* nbead, 1 or 2; NULL: all 1 */
+  int nbnd;   const int* bond_i; const int* bond_j; const float* bond_r0;
+  int nang;   const int* ang_i;  const int* ang_k;
+  int natt;   const int* att_i;  const int* att_j;  const float* att_r0; const float* att_eps;
+  long long nrep; const int* rep_i; const int* rep_j;
+} sop_energy_lists;
+int sop_energy_noalloc(const sop_params* p, const sop_energy_lists* l, double* terms, void* stream);
+/* Message of the last sop_energy_noalloc failure. */
+const char* sop_energy_noalloc_error(void);
+
 /* Last error message of the context (or of the library when ctx is NULL). */
 const char* sop_last_error(void* ctx);
 

@@ -20,7 +20,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["engine.cu", "kernels_lists.cu", "kernels_step.cu"]
+CU_SOURCES = ["engine.cu", "kernels_lists.cu", "kernels_step.cu", "energy_noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -65,6 +65,29 @@ class MoleculeDesc(ctypes.Structure):
                 ("T", ctypes.c_double), ("traj", ctypes.c_uint), ("nsteps", ctypes.c_longlong)]
 
 
+class EnergyLists(ctypes.Structure):
+    """sop_energy_lists: device pointers owned by the caller."""
+    _fields_ = [("nbead", ctypes.c_int), ("unc_pos", ctypes.c_void_p), ("types", ctypes.c_void_p),
+                ("nbnd", ctypes.c_int), ("bond_i", ctypes.c_void_p), ("bond_j", ctypes.c_void_p),
+                ("bond_r0", ctypes.c_void_p),
+                ("nang", ctypes.c_int), ("ang_i", ctypes.c_void_p), ("ang_k", ctypes.c_void_p),
+                ("natt", ctypes.c_int), ("att_i", ctypes.c_void_p), ("att_j", ctypes.c_void_p),
+                ("att_r0", ctypes.c_void_p), ("att_eps", ctypes.c_void_p),
+                ("nrep", ctypes.c_longlong), ("rep_i", ctypes.c_void_p), ("rep_j", ctypes.c_void_p)]
+
+
+ENERGY_NOALLOC_MAX_ITEMS = 4194304
+
+
+def energy_noalloc(params: "Params", lists: EnergyLists, terms_ptr: int, stream: int = 0) -> None:
+    """sop_energy_noalloc: energy terms of caller-owned device lists into the
+    caller-owned device array at terms_ptr (5 doubles); allocates nothing."""
+    rc = lib().sop_energy_noalloc(ctypes.byref(params), ctypes.byref(lists),
+                                  ctypes.c_void_p(terms_ptr), ctypes.c_void_p(stream))
+    if rc != SOP_OK:
+        raise SopError(rc, (lib().sop_energy_noalloc_error() or b"").decode())
+
+
 def lib_path() -> str:
     return os.path.join(_HERE, "libsopgpu.so")
 
@@ -114,6 +137,8 @@ def lib() -> ctypes.CDLL:
             "sop_serve_result": (I, [V, I, V, V, V, ctypes.POINTER(I), PLL,
                                      ctypes.POINTER(ctypes.c_double)]),
             "sop_serve_stats": (I, [V, V]),
+            "sop_energy_noalloc": (I, [ctypes.POINTER(Params), ctypes.POINTER(EnergyLists), V, V]),
+            "sop_energy_noalloc_error": (ctypes.c_char_p, []),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
