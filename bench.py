@@ -200,6 +200,157 @@ def cpu_baseline(mols, ts, seconds_target: float = 15.0) -> dict:
                       f"force kernels and integrator, one trajectory per thread"}
 
 
+SERVED_RATE = 200.0          # jobs/s (Poisson)
+SERVED_SECONDS = 1.0         # arrival window
+SERVED_STEPS = (2e2, 2e4)    # the served stream's step range [1e4, 1e6] scaled by 1/50
+SERVED_BUDGET = 16 << 30     # device bytes for coordinates, velocities, topology, lists
+SERVED_BOXL = 1.0e6          # holds a fully extended 20,000-bead chain without self-images
+
+
+def served_stream(local: int) -> dict:
+    """Continuous batching on a Poisson request stream, then the same jobs'
+    plain-path speed (a sample run one at a time)."""
+    from sop_gb300 import engine
+    req = system.request_stream(SERVED_RATE, SERVED_SECONDS, (50, 20000), SERVED_STEPS,
+                                (0.5, 0.8), seed=5)
+    njob = len(req["n"])
+    mols = [system.generate(int(n), 100000 + k) for k, n in enumerate(req["n"])]
+    xyz = [m.extended_xyz() if req["extended"][k] else m.xyz for k, m in enumerate(mols)]
+    p = engine.baseline_params(device=local, boxl=SERVED_BOXL)
+    lat, work, statuses = {}, 0, []
+    with engine.Server(p, SERVED_BUDGET, 20000) as srv:
+        ids = {}
+        nxt = 0
+        t0 = time.perf_counter()
+        while len(lat) < njob:
+            now = time.perf_counter() - t0
+            if now > 900.0:
+                raise RuntimeError("served stream did not drain in 900 s")
+            while nxt < njob and req["arrival"][nxt] <= now:
+                ids[srv.submit(mols[nxt], xyz[nxt], int(req["steps"][nxt]), float(req["T"][nxt]),
+                               traj=nxt)] = nxt
+                nxt += 1
+            s = srv.stats()
+            if s["queued"] == 0 and s["active"] == 0 and nxt < njob:
+                time.sleep(max(0.0, min(1e-3, req["arrival"][nxt] - now)))
+                continue
+            srv.advance(1)
+            for j in srv.finished():
+                r = srv.result(j)
+                k = ids[j]
+                lat[k] = r["latency_s"]
+                work += int(req["n"][k]) * int(r["steps"])
+                statuses.append(r["status"])
+        wall = time.perf_counter() - t0
+        stats = srv.stats()
+    served_rate = work / wall
+    # the plain path on every 10th job, one context at a time
+    sample = list(range(0, njob, 10))
+    pw, pt = 0, 0.0
+    for k in sample:
+        ep = engine.plain(mols[k], xyz[k], p, T=float(req["T"][k]), traj=k,
+                          nsteps=int(req["steps"][k]))
+        t1 = time.perf_counter()
+        ep.step(int(req["steps"][k]))
+        pt += time.perf_counter() - t1
+        pw += int(req["n"][k]) * int(req["steps"][k])
+        ep.close()
+    lv = np.array([lat[k] for k in range(njob)])
+    return {"value": served_rate, "unit": UNIT,
+            "latency_p50_s": float(np.percentile(lv, 50)),
+            "latency_p99_s": float(np.percentile(lv, 99)),
+            "jobs": njob, "bead_steps": work, "wall_s": wall,
+            "plain_sequential": pw / pt, "served_over_plain": served_rate / (pw / pt),
+            "failed_jobs": int(sum(1 for s in statuses if s & 3)),
+            "device_bytes": stats["device_bytes"],
+            "config": f"Poisson {SERVED_RATE:.0f} jobs/s for {SERVED_SECONDS:.0f} s ({njob} jobs), "
+                      f"N log-uniform [50,20000], steps log-uniform [{SERVED_STEPS[0]:.0f},"
+                      f"{SERVED_STEPS[1]:.0f}] (the [1e4,1e6] range scaled by 1/50), kBT "
+                      f"U[0.5,0.8], half native / half extended, budget "
+                      f"{SERVED_BUDGET >> 30} GiB, boxl {SERVED_BOXL:.0f} A; plain_sequential: "
+                      f"every 10th job alone, one context at a time"}
+
+
+def plain_50k(args, local: int) -> None:
+    """The plain single-molecule path on the 50,000-bead structure (per-contact
+    epsilon in [0.7, 1.3]): whole-step rate and each stage's HBM roofline."""
+    import torch
+    from sop_gb300 import engine
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(local)
+    mol = system.generate(50000, 2, (0.7, 1.3))
+    p = engine.baseline_params(device=local, graph_steps=MD_STEPS)
+    e = engine.plain(mol, mol.xyz, p, T=0.6)
+    stream = torch.cuda.ExternalStream(e.stream(), device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        e.step_async(MD_STEPS)
+    e.sync()
+    K = args.steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(K)]
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            for k in range(K):
+                flush.zero_()
+                ev[k][0].record(stream)
+                e.step_async(MD_STEPS)
+                ev[k][1].record(stream)
+        torch.cuda.synchronize(dev)
+        e.sync()
+    t = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+    value = mol.n * MD_STEPS * K / t
+    ls = e.list_sizes()
+    N, B = mol.n, len(mol.bond_i)
+    peak, peak_kind = measured_peaks()
+    stage_bytes = {
+        # read x, v, f, incr; write x, p, v, incr, f (float4); bond r0; list entries
+        0: 112.0 * N + 4.0 * B + 4.0 * ls["nil_rep"] + 12.0 * ls["nil_att"],
+        # stream both directions of the NL rows and write the PL rows; counts and x_i
+        1: 24.0 * N + 8.0 * (ls["nnl_rep"] + ls["nil_rep"]) + 2.0 * (24.0 * ls["nnl_att"]
+                                                                 + 16.0 * ls["nil_att"]),
+        # cell binning (bbox, cells, sorted copy) + writing both directions of the NL
+        2: 64.0 * N + 8.0 * ls["nnl_rep"] + 8.0 * ls["nnl_att"],
+    }
+    names = {0: "fused force + Langevin step (k_step)", 1: "pair-list rebuild (k_pl)",
+             2: "neighbour-list rebuild (binning + k_nl)"}
+    stages = {}
+    for st in (0, 1, 2):
+        reps = 20
+        kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(reps)]
+        with torch.cuda.stream(stream):
+            for k in range(reps):
+                flush.zero_()
+                kev[k][0].record(stream)
+                e.launch_stage(st, 0)
+                kev[k][1].record(stream)
+        torch.cuda.synchronize(dev)
+        tk = statistics.median(a.elapsed_time(b) for a, b in kev) / 1e3
+        ach = stage_bytes[st] / tk / 1e9
+        stages[names[st]] = {"us": tk * 1e6, "bytes": stage_bytes[st], "achieved_gbs": ach,
+                             "frac": ach / peak}
+    e.sync()
+    e.close()
+    s0 = stages[names[0]]
+    n_launch = sum(launches_per_bench_step(p, k * MD_STEPS) for k in range(K))
+    line = {"metric": "bead-steps/s (plain path, 50,000 beads)", "value": value, "unit": UNIT,
+            "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": 1e3 * t / K,
+            "higher_is_better": True, "scaling": "none", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "plain path, one molecule of 50,000 beads (seed 2), per-contact "
+                                   "epsilon U[0.7,1.3], NL 32 A / 50 steps, PL 16 A / 10 steps, "
+                                   "CUDA graph of 10 steps per replay",
+                       "md_steps_per_bench_step": MD_STEPS,
+                       "l2": "flushed before every timed step (256 MiB write)"},
+            "roofline": {"bound": "hbm", "achieved": s0["achieved_gbs"], "peak": peak,
+                         "unit": "GB/s", "frac": s0["frac"], "traffic": None,
+                         "kernel": names[0], "peak_source": peak_kind},
+            "stages": stages, "lists": ls, "gpu_launches": int(n_launch), "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, rank: int) -> None:
     from oracle import pyoracle as O
     mols, ts = ensemble(0)
@@ -251,6 +402,10 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-loop comparison")
+    ap.add_argument("--no-served", action="store_true", help="skip the served request stream")
+    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "plain50k"],
+                    help="ensemble: the batched ensemble (with the served stream beside it); "
+                         "plain50k: the plain path on the 50,000-bead structure")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -261,6 +416,11 @@ def main() -> None:
     if args.impl == "reference":
         if rank == 0:
             run_reference(args, rank)
+        return
+
+    if args.workload == "plain50k":
+        if rank == 0:
+            plain_50k(args, local)
         return
 
     import torch
@@ -393,6 +553,10 @@ def main() -> None:
                  "sample": f"{len(sample)} of the trajectories (every 8th), {nst} steps each, "
                            f"one plain context at a time (the reference's single-molecule loop)"}
 
+    served = None
+    if rank == 0 and not args.no_served:
+        served = served_stream(local)
+
     if rank == 0:
         n_launch = sum(launches_per_bench_step(p, s_start + k * MD_STEPS) for k in range(K))
         line = {
@@ -411,6 +575,7 @@ def main() -> None:
             "clocks": clk.summary(),
             "plain_loop": plain,
             "batched_over_plain": (value / world / plain["value"]) if plain else None,
+            "served": served,
             "lists": ls,
             "tuning": tuning,
             "molecule_errors": int(sum(1 for s in statuses if s & 3)),

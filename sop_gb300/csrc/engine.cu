@@ -288,7 +288,9 @@ int autotune_lanes(SopCtx* ctx) {
 int alloc_nl(SopCtx* ctx, long long stride) {
   stride = (stride + 31) / 32 * 32;  // rows stay 16-byte aligned
   const long long entries = stride * (long long)ctx->s.nbead;
-  if (entries > 0x7fffffffLL) return ctx->fail(SOP_ERR_CAPACITY, "neighbour list exceeds 2^31 entries");
+  // rows are addressed with 64-bit offsets; the bound only keeps the byte
+  // count (two int arrays) far from overflow
+  if (entries > (1LL << 40)) return ctx->fail(SOP_ERR_CAPACITY, "neighbour list exceeds 2^40 entries");
   ctx->dfree(ctx->s.nl_j);
   ctx->dfree(ctx->s.pl_j);
   ctx->s.nl_j = ctx->dalloc<int>(entries);
@@ -994,9 +996,11 @@ int sop_serve_create(const sop_params* p, long long budget_bytes, long long max_
   int P = graph_steps(ctx);
   if (ctx->P.nnlup % P) ctx->P.graph_steps = std::gcd(P, ctx->P.nnlup);
   set_constants(ctx);
-  // list rows: about 1.3 x the neighbours of a bead in a dense (2.8e-3 / A^3) globule
+  // list rows: 1.3 x the neighbours of a bead in the densest part of a
+  // globule (6e-3 / A^3: the cores of the synthetic structures reach about
+  // twice their mean density of 2.5e-3), so rows rarely have to regrow
   const double rc_nl = ctx->s.rc_nl_rep_max;
-  long long stride = (long long)(1.3 * 2.8e-3 * 4.18879 * rc_nl * rc_nl * rc_nl) + 32;
+  long long stride = (long long)(1.3 * 6.0e-3 * 4.18879 * rc_nl * rc_nl * rc_nl) + 32;
   stride = std::max<long long>(64, (stride + 31) / 32 * 32);
   // bytes per bead slot: state (8 float4), counters and cell data (10 ints),
   // rows (3 int2), topology (2 bond, 2 angle, 8 native entries) and list rows
