@@ -15,8 +15,8 @@
 //      predicate = the reference's FP32 host filter (d^2 < rcut^2, |i-j| > 2,
 //      not native); one pass writes fixed-stride rows (overflow: regrow) k_nl
 //   The attractive neighbour list filters each bead's native row (k_assign).
-// Pair list (every nplup steps): warp per bead compacts its neighbour-list row
-// in place order (k_pl).
+// Pair list (every nplup steps): eight lanes per bead compact its
+// neighbour-list row in place order (k_pl).
 #include "sop_dev.cuh"
 
 namespace sop {
@@ -414,16 +414,20 @@ __global__ void __launch_bounds__(256) k_nl(DevSys s) {
   }
 }
 
-// Warp per bead: the pair list is the in-order compaction of the bead's
-// neighbour-list row by the pair-list cut-off (sop.cu:835-920 semantics,
-// host arithmetic of sop.cu:1737-1810).  Each lane takes 4 consecutive
-// entries per iteration (one 16-byte load, four independent gathers) and a
-// warp scan places the survivors; the attractive pair list is the same over
-// the bead's attractive neighbour list.
+// kPlLanes lanes per bead (four beads per warp): the pair list is the
+// in-order compaction of the bead's neighbour-list row by the pair-list
+// cut-off (sop.cu:835-920 semantics, host arithmetic of sop.cu:1737-1810).
+// Each lane takes 4 consecutive entries per round (one 16-byte load, four
+// independent gathers) and a scan across the group places the survivors;
+// the attractive pair list is the same over the bead's attractive
+// neighbour list.
+constexpr int kPlLanes = 8;   // lanes per bead in the pair-list rebuild
 __global__ void __launch_bounds__(256) k_pl(DevSys s, int koff) {
-  const int lane = threadIdx.x & 31;
-  // beads in cell order: the warps of a block gather from the same region
-  const int kk = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int wl = threadIdx.x & 31;
+  const int lane = wl & (kPlLanes - 1);
+  const unsigned gmask = ((1u << kPlLanes) - 1u) << (wl & ~(kPlLanes - 1));
+  // beads in cell order: the groups of a block gather from the same region
+  const int kk = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) / kPlLanes);
   if (kk >= s.cell_start[s.cell_cap]) return;
   if (*s.flags & FLAG_NL_OVERFLOW) return;
   const int i = s.sorted[kk];
@@ -442,37 +446,38 @@ __global__ void __launch_bounds__(256) k_pl(DevSys s, int koff) {
   const int2 row = s.nat_row[i];
   const int acnt = s.nl_att_cnt[i];
   int k = 0;
-  for (int e0 = 0; e0 < cnt; e0 += 128) {
+  for (int e0 = 0; e0 < cnt; e0 += 4 * kPlLanes) {
     const int e = e0 + 4 * lane;
     int4 jv = make_int4(i, i, i, i);
     if (e < cnt) jv = row4[(e0 >> 2) + lane];
     const int jq[4] = {jv.x, e + 1 < cnt ? jv.y : i, e + 2 < cnt ? jv.z : i, e + 3 < cnt ? jv.w : i};
-    bool pq[4];
+    unsigned pb = 0;
     int c = 0;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const float4 xj = X[e + q < cnt ? jq[q] : i];
+      const float4 xj = X[jq[q]];
       float dx = __fsub_rn(xj.x, xi.x), dy = __fsub_rn(xj.y, xi.y),
             dz = __fsub_rn(xj.z, xi.z);
       min_image3(dx, dy, dz, boxl);
-      pq[q] = (e + q < cnt) && d2_exact(dx, dy, dz) < pick_type_pair(r11, r12, r22, ti, type_of(xj));
-      c += pq[q] ? 1 : 0;
+      const bool p = (e + q < cnt) && d2_exact(dx, dy, dz) < pick_type_pair(r11, r12, r22, ti, type_of(xj));
+      pb |= (p ? 1u : 0u) << q;
+      c += p ? 1 : 0;
     }
     int incl = c;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    for (int o = 1; o < kPlLanes; o <<= 1) {
+      const int t = __shfl_up_sync(gmask, incl, o, kPlLanes);
       if (lane >= o) incl += t;
     }
     int pos = k + incl - c;
 #pragma unroll
     for (int q = 0; q < 4; ++q)
-      if (pq[q]) out[pos++] = jq[q];
-    k += __shfl_sync(0xffffffffu, incl, 31);
+      if (pb & (1u << q)) out[pos++] = jq[q];
+    k += __shfl_sync(gmask, incl, kPlLanes - 1, kPlLanes);
   }
   if (lane == 0) s.pl_cnt[i] = k;
   int ka = 0;
-  for (int e0 = 0; e0 < acnt; e0 += 32) {
+  for (int e0 = 0; e0 < acnt; e0 += kPlLanes) {
     const int e = e0 + lane;
     bool pass = false;
     int idx = 0, j = 0;
@@ -485,7 +490,7 @@ __global__ void __launch_bounds__(256) k_pl(DevSys s, int koff) {
       min_image3(dx, dy, dz, boxl);
       pass = d2_exact(dx, dy, dz) < s.nat_rc2[idx].y;
     }
-    const unsigned mask = __ballot_sync(0xffffffffu, pass);
+    const unsigned mask = (__ballot_sync(gmask, pass) >> (wl & ~(kPlLanes - 1))) & ((1u << kPlLanes) - 1u);
     if (pass) {
       float4 q = s.nat_par[idx];
       s.pl_att[row.x + ka + __popc(mask & lt)] = make_float4(__int_as_float(j), q.x, q.y, q.z);
@@ -531,7 +536,7 @@ void launch_nl_rebuild(const DevSys& s, const NLScratch& w, int koff, cudaStream
 
 void launch_pl_rebuild(const DevSys& s, int koff, cudaStream_t st) {
   const int T = 256;
-  k_pl<<<cdiv((long long)s.nbead * 32, T), T, 0, st>>>(s, koff);
+  k_pl<<<cdiv((long long)s.nbead * kPlLanes, T), T, 0, st>>>(s, koff);
 }
 
 }  // namespace sop

@@ -24,10 +24,69 @@ namespace sop {
 
 constexpr int kV = 16;  // virtual lanes of the fixed force-summation order
 
+// Blocks per SM each lane-group width is compiled for (a register cap).
+template <int G>
+struct StepBlocks {
+  static constexpr int value = G == 4 ? 5 : (G == 8 ? 6 : (G == 16 ? 4 : 1));
+};
+
+// Every rounding of the per-entry arithmetic and of the accumulation is
+// written out (one rounding per operation), so the compiler cannot contract
+// it differently in different instantiations: the sums are then the same
+// bits for every lane-group width.
+__device__ __forceinline__ void acc3(float& ax, float& ay, float& az, float c, float dx, float dy,
+                                     float dz) {
+  ax = __fmaf_rn(c, dx, ax);
+  ay = __fmaf_rn(c, dy, ay);
+  az = __fmaf_rn(c, dz, az);
+}
+
+__device__ __forceinline__ float d2_plain(float dx, float dy, float dz) {
+  return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// Force coefficient of one bonded / angle / native entry (type 0 / 1 / 2):
+// the reference kernels' formulas, with the compensated d^2 - r0^2 wherever
+// a difference from the native distance enters.
+__device__ __forceinline__ float small_coeff(const DevSys& s, int type, float dx, float dy, float dz,
+                                             float lx, float ly, float lz, float r0, float eps,
+                                             bool& fene_bad) {
+  const float d2 = d2_plain(dx, dy, dz);
+  if (type == 0) {
+    // FENE: force on i = +k dev / (r (1 - dev^2/R0^2)) * d  (energy.cu:252-271);
+    // dev carries the compensated d^2 - r0^2, so approximate reciprocals
+    // (a few ulps) keep the term well inside the force tolerance
+    const float r = __fmul_rn(d2, rsqrtf(d2));
+    const float dev = __fmul_rn(d2_minus_r02(dx, dy, dz, lx, ly, lz, r0),
+                                __fdividef(1.0f, __fadd_rn(r, r0)));
+    const float w = __fsub_rn(1.0f, __fmul_rn(__fmul_rn(dev, dev), s.inv_R0sq));
+    fene_bad |= !(fabsf(dev) < s.R0);
+    return __fmul_rn(__fmul_rn(s.k_bnd, dev), __fdividef(1.0f, __fmul_rn(r, w)));
+  }
+  if (type == 1) {
+    // i,i+2 soft sphere: force on i = -6 eps sigma^6 / d^8 * d  (energy.cu:335-360)
+    const float inv = __fdividef(1.0f, d2);
+    const float inv2 = __fmul_rn(inv, inv);
+    return __fmul_rn(-s.f_ss, __fmul_rn(inv2, inv2));
+  }
+  // native LJ 12-6 (energy.cu:468-507): co1 = -12 eps / d^2 (s^6 - s^3),
+  // s = r0^2 / d^2, as -12 eps / d^2 s^3 (s - 1)(s^2 + s + 1) with
+  // s - 1 = -(d^2 - r0^2) / d^2; pairs with d^2 <= 1e-7 r0^2 are skipped.
+  const float r02 = __fmul_rn(r0, r0);
+  const float inv = __fdividef(1.0f, d2);
+  const float sr = __fmul_rn(r02, inv);
+  const float sm1 = __fmul_rn(-d2_minus_r02(dx, dy, dz, lx, ly, lz, r0), inv);
+  const float s3 = __fmul_rn(__fmul_rn(sr, sr), sr);
+  const float poly = __fadd_rn(__fadd_rn(__fmul_rn(sr, sr), sr), 1.0f);
+  const float c =
+      __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(-12.0f, eps), inv), __fmul_rn(s3, sm1)), poly);
+  return d2 > __fmul_rn(1.0e-7f, r02) ? c : 0.0f;
+}
+
 // STEP = false: force evaluation only at step mol_step + koff (velocities kept),
 // followed by the look-ahead; used after set-up and state uploads.
 template <int G, bool STEP, bool UNI>
-__global__ void __launch_bounds__(256) k_step(DevSys s, int koff) {
+__global__ void __launch_bounds__(256, StepBlocks<G>::value) k_step(DevSys s, int koff) {
   constexpr int BPB = 256 / G;          // beads per block
   __shared__ float4 fsum[BPB];          // conservative force sums; w = FENE range flag
   __shared__ int bead[BPB];             // bead of each slot, -1: nothing to do
@@ -82,52 +141,29 @@ __global__ void __launch_bounds__(256) k_step(DevSys s, int koff) {
       for (int c = 0; c < kC; ++c) {
         const int e = base + lane + c * G;
         if (e >= nsmall) continue;
-        int j;
+        int j, t;
         float r0 = 0.f, eps = 0.f;
         if (e < br.y) {
           j = s.bond_j[br.x + e];
           r0 = s.bond_r0[br.x + e];
+          t = 0;
         } else if (e < nba) {
           j = s.ang_j[ar.x + e - br.y];
+          t = 1;
         } else {
           const float4 q = s.pl_att[abase + e - nba];
           j = __float_as_int(q.x);
           r0 = q.y;
           eps = q.z;
+          t = 2;
         }
         const float4 xj = X[j];
         float lx, ly, lz;
         float dx = diff_exact(xj.x, xi.x, lx), dy = diff_exact(xj.y, xi.y, ly),
               dz = diff_exact(xj.z, xi.z, lz);
         min_image3(dx, dy, dz, boxl);
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        float cc;
-        if (e < br.y) {
-          // FENE: force on i = +k dev / (r (1 - dev^2/R0^2)) * d  (energy.cu:252-271);
-          // dev carries the compensated d^2 - r0^2, so approximate reciprocals
-          // (a few ulps) keep the term well inside the force tolerance
-          const float r = d2 * rsqrtf(d2);
-          const float dev = d2_minus_r02(dx, dy, dz, lx, ly, lz, r0) * __fdividef(1.0f, r + r0);
-          const float w = 1.0f - dev * dev * s.inv_R0sq;
-          fene_bad |= !(fabsf(dev) < s.R0);
-          cc = s.k_bnd * dev * __fdividef(1.0f, r * w);
-        } else if (e < nba) {
-          // i,i+2 soft sphere: force on i = -6 eps sigma^6 / d^8 * d  (energy.cu:335-360)
-          const float inv = __fdividef(1.0f, d2);
-          const float inv2 = inv * inv;
-          cc = -s.f_ss * inv2 * inv2;
-        } else {
-          // native LJ 12-6 (energy.cu:468-507): co1 = -12 eps / d^2 (s^6 - s^3),
-          // s = r0^2 / d^2, as -12 eps / d^2 s^3 (s - 1)(s^2 + s + 1) with
-          // s - 1 = -(d^2 - r0^2) / d^2; pairs with d^2 <= 1e-7 r0^2 are skipped.
-          const float r02 = r0 * r0;
-          const float inv = __fdividef(1.0f, d2);
-          const float sr = r02 * inv;
-          const float sm1 = -d2_minus_r02(dx, dy, dz, lx, ly, lz, r0) * inv;
-          const float s3 = sr * sr * sr;
-          cc = (d2 > 1.0e-7f * r02) ? -12.0f * eps * inv * s3 * sm1 * (sr * sr + sr + 1.0f) : 0.0f;
-        }
-        ax[c] += cc * dx; ay[c] += cc * dy; az[c] += cc * dz;
+        const float cc = small_coeff(s, t, dx, dy, dz, lx, ly, lz, r0, eps, fene_bad);
+        acc3(ax[c], ay[c], az[c], cc, dx, dy, dz);
       }
     }
 
@@ -156,10 +192,11 @@ __global__ void __launch_bounds__(256) k_step(DevSys s, int koff) {
       for (int c = 0; c < kC; ++c) {
         // past the row end xx[c] is bead i itself: d2 = 0 fails the tolerance
         // test and contributes exactly 0, so no branch is needed
-        float dx = xx[c].x - xi.x, dy = xx[c].y - xi.y, dz = xx[c].z - xi.z;
+        float dx = __fsub_rn(xx[c].x, xi.x), dy = __fsub_rn(xx[c].y, xi.y),
+              dz = __fsub_rn(xx[c].z, xi.z);
         // |dx| + |dy| + |dz| bounds every component: one test for the rare wrap
         if (fabsf(dx) + fabsf(dy) + fabsf(dz) > q4) min_image3(dx, dy, dz, boxl);
-        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float d2 = d2_plain(dx, dy, dz);
         float sg2 = g11, tol = t11;
         if (!UNI) {
           const int tj = type_of(xx[c]);
@@ -167,10 +204,11 @@ __global__ void __launch_bounds__(256) k_step(DevSys s, int koff) {
           tol = pick_type_pair(t11, t12, t22, ti, tj);
         }
         const float inv = __fdividef(1.0f, d2);
-        const float u = sg2 * inv;
-        const float u3 = u * u * u;
-        const float cc = (d2 > tol) ? ce * inv * u3 * (two * u3 + 1.0f) : 0.0f;
-        ax[c] += cc * dx; ay[c] += cc * dy; az[c] += cc * dz;
+        const float u = __fmul_rn(sg2, inv);
+        const float u3 = __fmul_rn(__fmul_rn(u, u), u);
+        const float cc = (d2 > tol) ? __fmul_rn(__fmul_rn(__fmul_rn(ce, inv), u3), __fmaf_rn(two, u3, 1.0f))
+                                    : 0.0f;
+        acc3(ax[c], ay[c], az[c], cc, dx, dy, dz);
       }
     }
     // upper levels of the fixed tree inside the lane, lower levels by shuffles
@@ -179,13 +217,17 @@ __global__ void __launch_bounds__(256) k_step(DevSys s, int koff) {
       const int oc = off / G;
 #pragma unroll
       for (int c = 0; c < kC; ++c)
-        if (c < oc) { ax[c] += ax[c + oc]; ay[c] += ay[c + oc]; az[c] += az[c + oc]; }
+        if (c < oc) {
+          ax[c] = __fadd_rn(ax[c], ax[c + oc]);
+          ay[c] = __fadd_rn(ay[c], ay[c + oc]);
+          az[c] = __fadd_rn(az[c], az[c + oc]);
+        }
     }
 #pragma unroll
     for (int off = G / 2; off > 0; off >>= 1) {
-      ax[0] += __shfl_xor_sync(gmask, ax[0], off);
-      ay[0] += __shfl_xor_sync(gmask, ay[0], off);
-      az[0] += __shfl_xor_sync(gmask, az[0], off);
+      ax[0] = __fadd_rn(ax[0], __shfl_xor_sync(gmask, ax[0], off));
+      ay[0] = __fadd_rn(ay[0], __shfl_xor_sync(gmask, ay[0], off));
+      az[0] = __fadd_rn(az[0], __shfl_xor_sync(gmask, az[0], off));
     }
     fene_bad = __any_sync(gmask, fene_bad);
   }
