@@ -271,14 +271,22 @@ def served_stream(local: int) -> dict:
                       f"every 10th job alone, one context at a time"}
 
 
-def plain_50k(args, local: int) -> None:
-    """The plain single-molecule path on the 50,000-bead structure (per-contact
-    epsilon in [0.7, 1.3]): whole-step rate and each stage's HBM roofline."""
+PLAIN = {  # workload: (beads, structure seed, per-contact epsilon range)
+    "plain128": (128, 0, None),
+    "plain4000": (4000, 1, None),
+    "plain50k": (50000, 2, (0.7, 1.3)),
+}
+
+
+def plain_one(args, local: int) -> None:
+    """The plain single-molecule path on one synthetic structure: whole-step
+    rate and each stage's HBM roofline."""
     import torch
     from sop_gb300 import engine
     dev = torch.device("cuda", local)
     torch.cuda.set_device(local)
-    mol = system.generate(50000, 2, (0.7, 1.3))
+    nbead, seed, eps = PLAIN[args.workload]
+    mol = system.generate(nbead, seed, eps)
     p = engine.baseline_params(device=local, graph_steps=MD_STEPS)
     e = engine.plain(mol, mol.xyz, p, T=0.6)
     stream = torch.cuda.ExternalStream(e.stream(), device=dev)
@@ -335,18 +343,38 @@ def plain_50k(args, local: int) -> None:
     e.close()
     s0 = stages[names[0]]
     n_launch = sum(launches_per_bench_step(p, k * MD_STEPS) for k in range(K))
-    line = {"metric": "bead-steps/s (plain path, 50,000 beads)", "value": value, "unit": UNIT,
+    cpu = None
+    if not args.no_cpu_baseline:
+        # the reference algorithm on one host core, in whole neighbour-list
+        # periods (50 steps, one O(N^2) list build each) until ~5 s have passed
+        from oracle import pyoracle as O
+        r = O.RefRun(mol, mol.xyz, CUT, 0.05, 0.05, 0.6, 50, 10, 1234, 0)
+        r.advance(0)
+        done, t_cpu = 0, 0.0
+        while t_cpu < 5.0:
+            t0 = time.perf_counter()
+            r.advance(50)
+            t_cpu += time.perf_counter() - t0
+            done += 50
+        r.close()
+        cpu = {"value": mol.n * done / t_cpu, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{done} Langevin steps of this molecule (whole 50-step neighbour-list "
+                         f"periods), serial FP32 restatement of the reference's host list filters, "
+                         f"force kernels and integrator, one thread"}
+    line = {"metric": f"bead-steps/s (plain path, {nbead:,} beads)", "value": value, "unit": UNIT,
             "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": 1e3 * t / K,
             "higher_is_better": True, "scaling": "none", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": "plain path, one molecule of 50,000 beads (seed 2), per-contact "
-                                   "epsilon U[0.7,1.3], NL 32 A / 50 steps, PL 16 A / 10 steps, "
+            "config": {"workload": f"plain path, one molecule of {nbead:,} beads (seed {seed})"
+                                   + (", per-contact epsilon U[0.7,1.3]" if eps else "")
+                                   + ", NL 32 A / 50 steps, PL 16 A / 10 steps, "
                                    "CUDA graph of 10 steps per replay",
                        "md_steps_per_bench_step": MD_STEPS,
                        "l2": "flushed before every timed step (256 MiB write)"},
             "roofline": {"bound": "hbm", "achieved": s0["achieved_gbs"], "peak": peak,
                          "unit": "GB/s", "frac": s0["frac"], "traffic": None,
                          "kernel": names[0], "peak_source": peak_kind},
+            "cpu_baseline": cpu,
             "stages": stages, "lists": ls, "gpu_launches": int(n_launch), "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 
@@ -403,9 +431,9 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-loop comparison")
     ap.add_argument("--no-served", action="store_true", help="skip the served request stream")
-    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "plain50k"],
+    ap.add_argument("--workload", default="ensemble", choices=["ensemble", *PLAIN],
                     help="ensemble: the batched ensemble (with the served stream beside it); "
-                         "plain50k: the plain path on the 50,000-bead structure")
+                         "plain128 / plain4000 / plain50k: the plain path on one structure")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -418,9 +446,9 @@ def main() -> None:
             run_reference(args, rank)
         return
 
-    if args.workload == "plain50k":
+    if args.workload in PLAIN:
         if rank == 0:
-            plain_50k(args, local)
+            plain_one(args, local)
         return
 
     import torch

@@ -263,6 +263,33 @@ int sop_serve_result(void* ctx, int job, float* unc_pos, float* vel, double* ene
 int sop_serve_stats(void* ctx, long long* out);
 
 /*
+ * Exact checkpoints.  The reference saves coordinates and velocities
+ * (save_coords / save_vels, io.cpp:261-381, called from sop.cu:268-272) and
+ * restarts from them; its GPU random state is not saved.  A checkpoint here
+ * holds everything the following steps read: the step counter and status,
+ * the coordinates of the last completed step and the look-ahead of the next,
+ * velocities, increments and forces, and the molecule's neighbour- and
+ * pair-list rows.  Restored into a context with the same parameters and the
+ * same molecule (topology, T, trajectory id, seed), the continuation is
+ * bit-identical to the run it came from.
+ *
+ * sop_checkpoint: buf = NULL returns the size in *size; otherwise cap bytes
+ * at buf receive the checkpoint.  Plain and batched contexts.
+ * sop_restore: writes a checkpoint into molecule `mol` of a committed
+ * context.  The context has one step clock: the first restore into a
+ * context that has not stepped sets it to the checkpoint's step, later
+ * restores must carry that same step.
+ */
+int sop_checkpoint(void* ctx, int mol, void* buf, long long cap, long long* size);
+int sop_restore(void* ctx, int mol, const void* buf, long long size);
+/* Served contexts: the checkpoint of a running job (taken between rounds,
+ * when its step is a multiple of nnlup), and a job that continues from one
+ * (queued like sop_serve_submit; m describes the same molecule, m->nsteps is
+ * the job's total step budget). */
+int sop_serve_checkpoint(void* ctx, int job, void* buf, long long cap, long long* size);
+int sop_serve_resume(void* ctx, const sop_molecule* m, const void* buf, long long size, int* job);
+
+/*
  * Energy without allocation.  No counterpart in the reference: an extension
  * for callers that may not allocate device memory -- a host application whose
  * own memory manager owns every device byte, a loop that must not stall on the

@@ -31,6 +31,7 @@ struct NLScratch {
 };
 void launch_nl_rebuild(const DevSys& s, const NLScratch& w, int koff, cudaStream_t st);
 void launch_pl_rebuild(const DevSys& s, int koff, cudaStream_t st);
+void launch_rebin(const DevSys& s, const NLScratch& w, cudaStream_t st);
 void launch_scan(const int* in, long long n, int* out, int* block_sums, cudaStream_t st);
 long long scan_block_sums_needed(long long n);
 // kernels_step.cu
@@ -153,6 +154,8 @@ struct Job {
   double energy[5] = {0, 0, 0, 0, 0};
   int status = 0;
   long long steps = 0;
+  std::vector<char> resume;   // checkpoint to continue from (empty: start at step 0)
+  long long resume_step = 0;
 };
 
 double now_seconds() {
@@ -170,6 +173,7 @@ struct SopCtx {
 
   DevSys s{};
   std::vector<void*> allocs;
+  std::map<void*, size_t> alloc_bytes;
   long long bytes = 0;
   NLScratch w{};
   int G = 8;
@@ -189,6 +193,7 @@ struct SopCtx {
   std::deque<int> queue;          // queued job ids in arrival order
   std::vector<int> slot_job;      // job in each molecule slot, -1: free
   std::vector<int> finished_new;  // finished since the last sop_serve_finished
+  bool stepped = false;       // a step was queued since the context was committed
   long long host_step = 0;    // common step of plain / batched contexts
   long long target_step = 0;  // step every molecule should reach after the queued work
   std::map<std::string, Graph> graphs;
@@ -213,6 +218,7 @@ struct SopCtx {
       return nullptr;
     }
     allocs.push_back(p);
+    alloc_bytes[p] = b;
     bytes += (long long)b;
     return (T*)p;
   }
@@ -220,6 +226,11 @@ struct SopCtx {
     if (!p) return;
     auto it = std::find(allocs.begin(), allocs.end(), p);
     if (it != allocs.end()) allocs.erase(it);
+    auto sz = alloc_bytes.find(p);
+    if (sz != alloc_bytes.end()) {
+      bytes -= (long long)sz->second;
+      alloc_bytes.erase(sz);
+    }
     cudaFree(p);
   }
   void drop_graphs() {
@@ -385,6 +396,7 @@ int graph_steps(const SopCtx* ctx) {
 // Queues nsteps steps of every molecule (no synchronisation).
 int step_async(SopCtx* ctx, long long nsteps) {
   const int P = graph_steps(ctx);
+  if (nsteps > 0) ctx->stepped = true;
   long long s0 = ctx->host_step;
   long long left = nsteps;
   while (left > 0) {
@@ -917,6 +929,234 @@ static int retire(SopCtx* ctx, int slot, const std::vector<long long>& steps,
 }
 
 // One round: wait, retire, admit, queue nnlup steps.
+
+// ------------------------------------------------------------ checkpoints
+// An exact checkpoint of one molecule: its step counter and status, both
+// coordinate buffers (the last completed step and the look-ahead the next
+// step reads), both wrapped-coordinate buffers, velocities, increments and
+// forces, and its neighbour- and pair-list rows with bead and native indices
+// relative to the molecule.  Restoring writes all of it back, so the steps
+// that follow read exactly what they read in the run the checkpoint came
+// from (the noise is keyed by the step, and the lists are rebuilt on the
+// same cadence from the same coordinates): the continuation is the same
+// bits.  The reference saves coordinates and velocities (save_coords /
+// save_vels, io.cpp:261-381, from sop.cu:268-272) and restarts from them,
+// not exactly.
+struct CkptHeader {
+  char magic[4];
+  int version;
+  int n;             // beads
+  int nnat2;         // native row entries (both directions)
+  long long step;    // last completed step
+  int status;        // SOP_MOL_* bits
+  int pad;
+  long long cnt[4];  // row entries: attractive NL, attractive PL, repulsive NL, repulsive PL
+};
+const char kCkptMagic[4] = {'S', 'O', 'P', 'K'};
+constexpr int kCkptVersion = 1;
+
+long long ckpt_bytes(int n, const long long* cnt) {
+  return (long long)sizeof(CkptHeader) + 7LL * 16 * n + 16LL * n + 4 * cnt[0] + 16 * cnt[1] +
+         4 * cnt[2] + 4 * cnt[3];
+}
+
+// Regrows the repulsive list rows to at least `stride` entries, keeping
+// every row (the other molecules' lists stay valid).  Stream idle.
+int grow_nl_keep(SopCtx* ctx, long long stride) {
+  stride = (stride + 31) / 32 * 32;
+  DevSys& s = ctx->s;
+  if (stride <= s.nl_stride) return SOP_OK;
+  const long long nb = s.nbead, old = s.nl_stride, entries = stride * nb;
+  if (entries > (1LL << 40)) return ctx->fail(SOP_ERR_CAPACITY, "neighbour list exceeds 2^40 entries");
+  int* nj = ctx->dalloc<int>(entries);
+  int* pj = ctx->dalloc<int>(entries);
+  if (!nj || !pj) {
+    ctx->dfree(nj);
+    ctx->dfree(pj);
+    return ctx->fail(SOP_ERR_ALLOC, "neighbour-list allocation failed");
+  }
+  CK(cudaMemcpy2D(nj, 4 * stride, s.nl_j, 4 * old, 4 * old, nb, cudaMemcpyDeviceToDevice));
+  CK(cudaMemcpy2D(pj, 4 * stride, s.pl_j, 4 * old, 4 * old, nb, cudaMemcpyDeviceToDevice));
+  ctx->dfree(s.nl_j);
+  ctx->dfree(s.pl_j);
+  s.nl_j = nj;
+  s.pl_j = pj;
+  s.nl_stride = stride;
+  ctx->drop_graphs();  // kernel arguments changed
+  return SOP_OK;
+}
+
+// Serialises molecule slot `slot` (stream idle).
+int checkpoint_of(SopCtx* ctx, int slot, std::vector<char>& out) {
+  DevSys& s = ctx->s;
+  const HostMol& hm = ctx->mols[slot];
+  const int n = hm.n, o = hm.start;
+  const long long nn2 = 2LL * (long long)hm.ni.size();
+  CkptHeader h{};
+  std::memcpy(h.magic, kCkptMagic, 4);
+  h.version = kCkptVersion;
+  h.n = n;
+  h.nnat2 = (int)nn2;
+  CK(cudaMemcpy(&h.step, s.mol_step + slot, sizeof(long long), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&h.status, s.mol_status + slot, sizeof(int), cudaMemcpyDeviceToHost));
+  std::vector<int> cnt(4 * (size_t)n);
+  const int* src[4] = {s.nl_att_cnt, s.pl_att_cnt, s.nl_cnt, s.pl_cnt};
+  for (int t = 0; t < 4; ++t) {
+    CK(cudaMemcpy(cnt.data() + (size_t)t * n, src[t] + o, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    h.cnt[t] = 0;
+    for (int i = 0; i < n; ++i) h.cnt[t] += cnt[(size_t)t * n + i];
+  }
+  out.assign((size_t)ckpt_bytes(n, h.cnt), 0);
+  char* w = out.data();
+  auto put = [&](const void* p, size_t b) {
+    std::memcpy(w, p, b);
+    w += b;
+  };
+  put(&h, sizeof h);
+  const int cur = (int)(h.step & 1);
+  const float4* arr[7] = {s.x[cur] + o, s.x[cur ^ 1] + o, s.p[cur] + o, s.p[cur ^ 1] + o,
+                          s.v + o, s.incr + o, s.f + o};
+  std::vector<float4> tmp(n);
+  for (int a = 0; a < 7; ++a) {
+    CK(cudaMemcpy(tmp.data(), arr[a], sizeof(float4) * n, cudaMemcpyDeviceToHost));
+    put(tmp.data(), sizeof(float4) * n);
+  }
+  put(cnt.data(), sizeof(int) * 4 * (size_t)n);
+  std::vector<int2> nrow(n);
+  CK(cudaMemcpy(nrow.data(), s.nat_row + o, sizeof(int2) * n, cudaMemcpyDeviceToHost));
+  std::vector<int> ae(nn2 > 0 ? nn2 : 1);
+  std::vector<float4> ap(nn2 > 0 ? nn2 : 1);
+  if (nn2) {
+    CK(cudaMemcpy(ae.data(), s.nl_att_e + hm.off_n, sizeof(int) * nn2, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ap.data(), s.pl_att + hm.off_n, sizeof(float4) * nn2, cudaMemcpyDeviceToHost));
+  }
+  for (int i = 0; i < n; ++i)
+    for (int t = 0; t < cnt[i]; ++t) {
+      int v = ae[nrow[i].x - hm.off_n + t] - (int)hm.off_n;
+      put(&v, sizeof v);
+    }
+  for (int i = 0; i < n; ++i)
+    for (int t = 0; t < cnt[(size_t)n + i]; ++t) {
+      float4 q = ap[nrow[i].x - hm.off_n + t];
+      q.x = bits_f(bits_i(q.x) - o);
+      put(&q, sizeof q);
+    }
+  const long long stride = s.nl_stride;
+  std::vector<int> rows((size_t)(stride * n));
+  for (int r = 0; r < 2; ++r) {
+    CK(cudaMemcpy(rows.data(), (r == 0 ? s.nl_j : s.pl_j) + (long long)o * stride,
+                  sizeof(int) * rows.size(), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; ++i)
+      for (int t = 0; t < cnt[(size_t)(2 + r) * n + i]; ++t) {
+        int v = rows[(size_t)i * stride + t] - o;
+        put(&v, sizeof v);
+      }
+  }
+  return SOP_OK;
+}
+
+// Writes a checkpoint into molecule slot `slot` (installed, stream idle).
+int restore_into(SopCtx* ctx, int slot, const char* buf, long long len) {
+  DevSys& s = ctx->s;
+  const HostMol& hm = ctx->mols[slot];
+  const int n = hm.n, o = hm.start;
+  const long long nn2 = 2LL * (long long)hm.ni.size();
+  CkptHeader h;
+  if (!buf || len < (long long)sizeof h) return ctx->fail(SOP_ERR_ARG, "checkpoint too short");
+  std::memcpy(&h, buf, sizeof h);
+  if (std::memcmp(h.magic, kCkptMagic, 4) || h.version != kCkptVersion)
+    return ctx->fail(SOP_ERR_ARG, "not a checkpoint of this format");
+  if (h.n != n || h.nnat2 != nn2)
+    return ctx->fail(SOP_ERR_ARG, "checkpoint of a different molecule");
+  for (int t = 0; t < 4; ++t)
+    if (h.cnt[t] < 0) return ctx->fail(SOP_ERR_ARG, "corrupt checkpoint");
+  if (len != ckpt_bytes(n, h.cnt)) return ctx->fail(SOP_ERR_ARG, "checkpoint size mismatch");
+  const char* r = buf + sizeof h;
+  auto get = [&](void* p, size_t b) {
+    std::memcpy(p, r, b);
+    r += b;
+  };
+  std::vector<std::vector<float4>> arr(7, std::vector<float4>(n));
+  for (int a = 0; a < 7; ++a) get(arr[a].data(), sizeof(float4) * n);
+  std::vector<int> cnt(4 * (size_t)n);
+  get(cnt.data(), sizeof(int) * cnt.size());
+  std::vector<int2> nrow(n);
+  CK(cudaMemcpy(nrow.data(), s.nat_row + o, sizeof(int2) * n, cudaMemcpyDeviceToHost));
+  long long sum[4] = {0, 0, 0, 0};
+  int maxrow = 0;
+  for (int i = 0; i < n; ++i) {
+    for (int t = 0; t < 4; ++t) {
+      const int c = cnt[(size_t)t * n + i];
+      if (c < 0 || (t < 2 && c > nrow[i].y)) return ctx->fail(SOP_ERR_ARG, "corrupt checkpoint");
+      sum[t] += c;
+      if (t >= 2) maxrow = std::max(maxrow, c);
+    }
+  }
+  for (int t = 0; t < 4; ++t)
+    if (sum[t] != h.cnt[t]) return ctx->fail(SOP_ERR_ARG, "corrupt checkpoint");
+  std::vector<int> ae(nn2 > 0 ? nn2 : 1, 0);
+  std::vector<float4> ap(nn2 > 0 ? nn2 : 1, make_float4(0.f, 0.f, 0.f, 0.f));
+  for (int i = 0; i < n; ++i)
+    for (int t = 0; t < cnt[i]; ++t) {
+      int v;
+      get(&v, sizeof v);
+      if (v < 0 || v >= nn2) return ctx->fail(SOP_ERR_ARG, "corrupt checkpoint");
+      ae[nrow[i].x - hm.off_n + t] = v + (int)hm.off_n;
+    }
+  for (int i = 0; i < n; ++i)
+    for (int t = 0; t < cnt[(size_t)n + i]; ++t) {
+      float4 q;
+      get(&q, sizeof q);
+      const int j = bits_i(q.x);
+      if (j < 0 || j >= n) return ctx->fail(SOP_ERR_ARG, "corrupt checkpoint");
+      q.x = bits_f(j + o);
+      ap[nrow[i].x - hm.off_n + t] = q;
+    }
+  if (maxrow > s.nl_stride) {
+    int rc = grow_nl_keep(ctx, (long long)maxrow * 5 / 4 + 32);
+    if (rc) return rc;
+  }
+  const long long stride = s.nl_stride;
+  std::vector<int> rows[2];
+  for (int k = 0; k < 2; ++k) {
+    rows[k].assign((size_t)(stride * n), o);
+    for (int i = 0; i < n; ++i)
+      for (int t = 0; t < cnt[(size_t)(2 + k) * n + i]; ++t) {
+        int v;
+        get(&v, sizeof v);
+        if (v < 0 || v >= n) return ctx->fail(SOP_ERR_ARG, "corrupt checkpoint");
+        rows[k][(size_t)i * stride + t] = v + o;
+      }
+  }
+  const int cur = (int)(h.step & 1);
+  float4* dst[7] = {s.x[cur] + o, s.x[cur ^ 1] + o, s.p[cur] + o, s.p[cur ^ 1] + o,
+                    s.v + o, s.incr + o, s.f + o};
+  for (int a = 0; a < 7; ++a)
+    CK(cudaMemcpy(dst[a], arr[a].data(), sizeof(float4) * n, cudaMemcpyHostToDevice));
+  int* cdst[4] = {s.nl_att_cnt, s.pl_att_cnt, s.nl_cnt, s.pl_cnt};
+  for (int t = 0; t < 4; ++t)
+    CK(cudaMemcpy(cdst[t] + o, cnt.data() + (size_t)t * n, sizeof(int) * n, cudaMemcpyHostToDevice));
+  if (nn2) {
+    CK(cudaMemcpy(s.nl_att_e + hm.off_n, ae.data(), sizeof(int) * nn2, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s.pl_att + hm.off_n, ap.data(), sizeof(float4) * nn2, cudaMemcpyHostToDevice));
+  }
+  CK(cudaMemcpy(s.nl_j + (long long)o * stride, rows[0].data(), sizeof(int) * rows[0].size(),
+                cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s.pl_j + (long long)o * stride, rows[1].data(), sizeof(int) * rows[1].size(),
+                cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s.mol_step + slot, &h.step, sizeof(long long), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s.mol_status + slot, &h.status, sizeof(int), cudaMemcpyHostToDevice));
+  return SOP_OK;
+}
+
+// The header of a checkpoint, or false when buf does not hold one.
+bool ckpt_head(const void* buf, long long len, CkptHeader* h) {
+  if (!buf || len < (long long)sizeof(CkptHeader)) return false;
+  std::memcpy(h, buf, sizeof(CkptHeader));
+  return !std::memcmp(h->magic, kCkptMagic, 4) && h->version == kCkptVersion && h->step >= 0 &&
+         len == ckpt_bytes(h->n, h->cnt);
+}
+
 static int serve_round(SopCtx* ctx) {
   int rc = sync_checked(ctx);
   if (rc) return rc;
@@ -936,6 +1176,7 @@ static int serve_round(SopCtx* ctx) {
   // admission in arrival order; a job that does not fit yet lets the next
   // few (smaller) ones try
   int looked = 0;
+  bool rebin = false;
   for (auto it = ctx->queue.begin(); it != ctx->queue.end() && looked < 64 && !ctx->free_slots.empty();) {
     Job& jb = ctx->jobs[*it];
     const int slot = ctx->free_slots.back();
@@ -945,7 +1186,8 @@ static int serve_round(SopCtx* ctx) {
         ctx->s.uniform_type = 0;
         ctx->drop_graphs();  // kernel arguments changed
       }
-    rc = install(ctx, slot, ctx->mols[slot], -(long long)ctx->P.nnlup);
+    const bool resumed = !jb.resume.empty();
+    rc = install(ctx, slot, ctx->mols[slot], resumed ? jb.resume_step : -(long long)ctx->P.nnlup);
     if (rc == SOP_ERR_CAPACITY) {
       ctx->mols[slot] = HostMol();
       ++it;
@@ -953,12 +1195,25 @@ static int serve_round(SopCtx* ctx) {
       continue;
     }
     if (rc) return rc;
+    if (resumed) {
+      // the job continues at its checkpoint's step: its state and lists come
+      // from the checkpoint, and the beads join the cell order below
+      rc = restore_into(ctx, slot, jb.resume.data(), (long long)jb.resume.size());
+      if (rc) return rc;
+      jb.resume.clear();
+      jb.resume.shrink_to_fit();
+      rebin = true;
+    }
     ctx->free_slots.pop_back();
     ctx->slot_job[slot] = *it;
     jb.slot = slot;
     jb.state = Job::ACTIVE;
     jb.mol = HostMol();
     it = ctx->queue.erase(it);
+  }
+  if (rebin) {
+    launch_rebin(ctx->s, ctx->w, ctx->stream);
+    CK(cudaGetLastError());
   }
   bool any = false;
   for (int id : ctx->slot_job) any |= id >= 0;
@@ -1460,6 +1715,94 @@ int sop_molecule_status(void* p, int mol, int* status, long long* step) {
   if (mc.nsteps >= 0 && st >= mc.nsteps) flags |= SOP_MOL_DONE;
   if (status) *status = flags;
   if (step) *step = st;
+  return SOP_OK;
+}
+
+static int copy_out_ckpt(SopCtx* ctx, const std::vector<char>& blob, void* buf, long long cap,
+                         long long* size) {
+  if (size) *size = (long long)blob.size();
+  if (!buf) return SOP_OK;
+  if (cap < (long long)blob.size())
+    return ctx->fail(SOP_ERR_CAPACITY, "checkpoint buffer too small (query the size with buf = NULL)");
+  std::memcpy(buf, blob.data(), blob.size());
+  return SOP_OK;
+}
+
+int sop_checkpoint(void* p, int mol, void* buf, long long cap, long long* size) {
+  if (!p) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (ctx->served) return ctx->fail(SOP_ERR_ARG, "served contexts use sop_serve_checkpoint");
+  int rc = check_mol(ctx, mol);
+  if (rc) return rc;
+  rc = sync_checked(ctx);
+  if (rc) return rc;
+  std::vector<char> blob;
+  rc = checkpoint_of(ctx, mol, blob);
+  if (rc) return rc;
+  return copy_out_ckpt(ctx, blob, buf, cap, size);
+}
+
+int sop_restore(void* p, int mol, const void* buf, long long size) {
+  if (!p || !buf) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (ctx->served) return ctx->fail(SOP_ERR_ARG, "served contexts use sop_serve_resume");
+  int rc = check_mol(ctx, mol);
+  if (rc) return rc;
+  rc = sync_checked(ctx);
+  if (rc) return rc;
+  CkptHeader h;
+  if (!ckpt_head(buf, size, &h)) return ctx->fail(SOP_ERR_ARG, "not a checkpoint of this format");
+  const long long step = h.step;
+  // one clock per context: the first restore into a context that has not
+  // stepped sets it; later ones must match it
+  const bool set_clock = !ctx->stepped && ctx->host_step == 0;
+  if (!set_clock && step != ctx->host_step)
+    return ctx->fail(SOP_ERR_ARG, "checkpoint step differs from the context's step");
+  rc = restore_into(ctx, mol, static_cast<const char*>(buf), size);
+  if (rc) return rc;
+  if (set_clock) {
+    ctx->host_step = ctx->target_step = step;
+    CK(cudaMemcpy(ctx->s.sys_step, &step, sizeof(long long), cudaMemcpyHostToDevice));
+  }
+  return SOP_OK;
+}
+
+int sop_serve_checkpoint(void* p, int job, void* buf, long long cap, long long* size) {
+  if (!p) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (!ctx->served) return ctx->fail(SOP_ERR_ARG, "not a served context");
+  if (job < 0 || job >= (int)ctx->jobs.size()) return ctx->fail(SOP_ERR_NOT_FOUND, "unknown job");
+  if (ctx->jobs[job].state != Job::ACTIVE) return ctx->fail(SOP_ERR_ARG, "job is not running");
+  int rc = sync_checked(ctx);
+  if (rc) return rc;
+  std::vector<char> blob;
+  rc = checkpoint_of(ctx, ctx->jobs[job].slot, blob);
+  if (rc) return rc;
+  return copy_out_ckpt(ctx, blob, buf, cap, size);
+}
+
+int sop_serve_resume(void* p, const sop_molecule* m, const void* buf, long long size, int* job) {
+  if (!p || !m || !buf) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (!ctx->served) return ctx->fail(SOP_ERR_ARG, "not a served context");
+  CkptHeader h;
+  if (!ckpt_head(buf, size, &h)) return ctx->fail(SOP_ERR_ARG, "not a checkpoint of this format");
+  if (h.n != m->nbead || h.nnat2 != 2 * m->nnat)
+    return ctx->fail(SOP_ERR_ARG, "checkpoint of a different molecule");
+  const long long step = h.step;
+  // admission happens where the context's neighbour-list period starts, so
+  // the job's own cadence lines up only for steps at that phase -- where a
+  // served job's checkpoint is taken between rounds
+  if (step % ctx->P.nnlup != 0)
+    return ctx->fail(SOP_ERR_ARG, "a served job resumes from a step that is a multiple of nnlup");
+  if (m->nsteps < step) return ctx->fail(SOP_ERR_ARG, "checkpoint beyond the job's step budget");
+  int id = -1;
+  int rc = sop_serve_submit(p, m, &id);
+  if (rc) return rc;
+  Job& jb = ctx->jobs[id];
+  jb.resume.assign(static_cast<const char*>(buf), static_cast<const char*>(buf) + size);
+  jb.resume_step = step;
+  if (job) *job = id;
   return SOP_OK;
 }
 

@@ -176,6 +176,12 @@ __global__ void k_grid(DevSys s, int* __restrict__ ncell, int koff) {
   const float rc = s.rc_nl_rep_max;
   bool periodic = false;
   for (int a = 0; a < 3; ++a) periodic |= !(ext[a] + rc < s.boxl);  // also true for NaN extents
+  // Separations inside the box [lo, lo + ext] never exceed ext (rounding is
+  // monotone), so below boxl/4 the minimum image leaves them unchanged.  The
+  // margin of one cut-off covers the drift until the next rebuild, for the
+  // pair-list filters that use the same flag.
+  bool wrap = false;
+  for (int a = 0; a < 3; ++a) wrap |= !(ext[a] + rc < 0.25f * s.boxl);
   if (periodic || n <= 96) {
     // every pair is scanned; cells are chunks of 32 consecutive beads
     g.brute = 1;
@@ -206,6 +212,7 @@ __global__ void k_grid(DevSys s, int* __restrict__ ncell, int koff) {
     g.cs = cs;
     for (int a = 0; a < 3; ++a) g.lo[a] = lo[a];
   }
+  g.wrap = wrap ? 1 : 0;
   g.ncell = g.dims[0] * g.dims[1] * g.dims[2];
   s.grid[m] = g;
   ncell[m] = g.ncell;
@@ -238,7 +245,7 @@ __device__ __forceinline__ int cell_coord(float v, float lo, float cs, int dim) 
 
 // Per bead: cell index and slot (counting sort), plus the attractive
 // neighbour-list filter of its native row (sop.cu:704-759 semantics).
-__global__ void k_assign(DevSys s, int koff) {
+__global__ void k_assign(DevSys s, int koff, int att) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= s.nbead) return;
   int m = s.mol_of[i];
@@ -266,6 +273,7 @@ __global__ void k_assign(DevSys s, int koff) {
   }
   s.bead_cell[i] = c;
   s.bead_slot[i] = atomicAdd(s.cell_cnt + c, 1);
+  if (!att) return;  // binning only: the lists stay as they are
   int2 row = s.nat_row[i];
   int k = 0;
   for (int e = 0; e < row.y; ++e) {
@@ -310,7 +318,7 @@ __global__ void k_cellsort(DevSys s, int koff, const int* __restrict__ cells_tot
   }
 }
 
-constexpr int kNatRegs = 16;
+constexpr int kNatRegs = 16;  // native partners held in registers (the rest are read)
 constexpr int kNlLanes = 8;
 
 // Distance from v to the slab [a, a + w] (0 inside).
@@ -328,6 +336,7 @@ __device__ __forceinline__ float slab_dist(float v, float a, float w) {
 // written to the bead's fixed-stride row in candidate order (group ballot).
 // The culling is conservative (a 1e-3 A margin); membership is decided by the
 // exact predicate alone.  The bead's native partners sit in registers.
+template <bool UNI>
 __global__ void __launch_bounds__(256) k_nl(DevSys s) {
   const int k = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) / kNlLanes);
   const int lane = threadIdx.x % kNlLanes;
@@ -348,6 +357,7 @@ __global__ void __launch_bounds__(256) k_nl(DevSys s) {
   const int y0 = max(cy - g.S, 0), y1 = min(cy + g.S, ny - 1);
   const int x0 = max(cx - g.S, 0), x1 = min(cx + g.S, nx - 1);
   const float boxl = s.boxl;
+  const bool wrap = g.wrap != 0;
   const float r11 = s.rc2_nl_rep[1][1], r12 = s.rc2_nl_rep[1][2], r22 = s.rc2_nl_rep[2][2];
   const float rcm = s.rc_nl_rep_max * 1.0001f + 1.0e-3f;
   const float rcm2 = rcm * rcm;
@@ -385,8 +395,8 @@ __global__ void __launch_bounds__(256) k_nl(DevSys s) {
           if (abs(j - i) > 2) {
             float dx = __fsub_rn(xj.x, xi.x), dy2 = __fsub_rn(xj.y, xi.y),
                   dz2 = __fsub_rn(xj.z, xi.z);
-            min_image3(dx, dy2, dz2, boxl);
-            pass = d2_exact(dx, dy2, dz2) < pick_type_pair(r11, r12, r22, ti, wj & 3);
+            if (wrap) min_image3(dx, dy2, dz2, boxl);
+            pass = d2_exact(dx, dy2, dz2) < (UNI ? r11 : pick_type_pair(r11, r12, r22, ti, wj & 3));
             if (pass) {
               bool native = false;
 #pragma unroll
@@ -422,6 +432,7 @@ __global__ void __launch_bounds__(256) k_nl(DevSys s) {
 // the attractive pair list is the same over the bead's attractive
 // neighbour list.
 constexpr int kPlLanes = 8;   // lanes per bead in the pair-list rebuild
+template <bool UNI>
 __global__ void __launch_bounds__(256) k_pl(DevSys s, int koff) {
   const int wl = threadIdx.x & 31;
   const int lane = wl & (kPlLanes - 1);
@@ -437,6 +448,7 @@ __global__ void __launch_bounds__(256) k_pl(DevSys s, int koff) {
   const float4 xi = X[i];
   const int ti = type_of(xi);
   const float boxl = s.boxl;
+  const bool wrap = s.grid[m].wrap != 0;  // from the neighbour-list build, with a cut-off of margin
   const float r11 = s.rc2_pl_rep[1][1], r12 = s.rc2_pl_rep[1][2], r22 = s.rc2_pl_rep[2][2];
   const unsigned lt = (1u << lane) - 1u;
   const long long a = (long long)i * s.nl_stride;
@@ -458,8 +470,9 @@ __global__ void __launch_bounds__(256) k_pl(DevSys s, int koff) {
       const float4 xj = X[jq[q]];
       float dx = __fsub_rn(xj.x, xi.x), dy = __fsub_rn(xj.y, xi.y),
             dz = __fsub_rn(xj.z, xi.z);
-      min_image3(dx, dy, dz, boxl);
-      const bool p = (e + q < cnt) && d2_exact(dx, dy, dz) < pick_type_pair(r11, r12, r22, ti, type_of(xj));
+      if (wrap) min_image3(dx, dy, dz, boxl);
+      const bool p = (e + q < cnt) &&
+                     d2_exact(dx, dy, dz) < (UNI ? r11 : pick_type_pair(r11, r12, r22, ti, type_of(xj)));
       pb |= (p ? 1u : 0u) << q;
       c += p ? 1 : 0;
     }
@@ -487,7 +500,7 @@ __global__ void __launch_bounds__(256) k_pl(DevSys s, int koff) {
       float4 xj = X[j];
       float dx = __fsub_rn(xj.x, xi.x), dy = __fsub_rn(xj.y, xi.y),
             dz = __fsub_rn(xj.z, xi.z);
-      min_image3(dx, dy, dz, boxl);
+      if (wrap) min_image3(dx, dy, dz, boxl);
       pass = d2_exact(dx, dy, dz) < s.nat_rc2[idx].y;
     }
     const unsigned mask = (__ballot_sync(gmask, pass) >> (wl & ~(kPlLanes - 1))) & ((1u << kPlLanes) - 1u);
@@ -519,24 +532,45 @@ struct NLScratch {
   int* cells_total;  // one int: cells in use
 };
 
-// Full neighbour-list rebuild from the coordinates at step mol_step + koff.
-void launch_nl_rebuild(const DevSys& s, const NLScratch& w, int koff, cudaStream_t st) {
+// Cell binning of the molecules a rebuild at koff covers (the cell order the
+// step kernel and the pair-list rebuild walk); att = 1 also refreshes the
+// attractive neighbour lists.
+static void launch_binning(const DevSys& s, const NLScratch& w, int koff, int att, cudaStream_t st) {
   const int T = 256;
   k_bbox_reset<<<cdiv(s.nmol, T), T, 0, st>>>(s);
   k_bbox<<<cdiv(s.nbead, T), T, 0, st>>>(s, koff);
   k_grid<<<cdiv(s.nmol, T), T, 0, st>>>(s, w.ncell, koff);
   k_grid_base<<<1, 1024, 0, st>>>(s, w.ncell, w.cells_total);
   cudaMemsetAsync(s.cell_cnt, 0, sizeof(int) * (size_t)s.cell_cap, st);
-  k_assign<<<cdiv(s.nbead, T), T, 0, st>>>(s, koff);
+  k_assign<<<cdiv(s.nbead, T), T, 0, st>>>(s, koff, att);
   launch_scan(s.cell_cnt, s.cell_cap, s.cell_start, w.block_sums, st);
   k_scatter<<<cdiv(s.nbead, T), T, 0, st>>>(s);
   k_cellsort<<<cdiv(s.cell_cap, T), T, 0, st>>>(s, koff, w.cells_total);
-  k_nl<<<cdiv((long long)s.nbead * kNlLanes, T), T, 0, st>>>(s);
+}
+
+// Full neighbour-list rebuild from the coordinates at step mol_step + koff.
+void launch_nl_rebuild(const DevSys& s, const NLScratch& w, int koff, cudaStream_t st) {
+  const int T = 256;
+  launch_binning(s, w, koff, 1, st);
+  if (s.uniform_type)
+    k_nl<true><<<cdiv((long long)s.nbead * kNlLanes, T), T, 0, st>>>(s);
+  else
+    k_nl<false><<<cdiv((long long)s.nbead * kNlLanes, T), T, 0, st>>>(s);
+}
+
+// The cell order alone, every list untouched: puts molecules that arrive
+// with their lists (restored from a checkpoint) into the order the step
+// kernel walks.  The order decides no result.
+void launch_rebin(const DevSys& s, const NLScratch& w, cudaStream_t st) {
+  launch_binning(s, w, 0, 0, st);
 }
 
 void launch_pl_rebuild(const DevSys& s, int koff, cudaStream_t st) {
   const int T = 256;
-  k_pl<<<cdiv((long long)s.nbead * kPlLanes, T), T, 0, st>>>(s, koff);
+  if (s.uniform_type)
+    k_pl<true><<<cdiv((long long)s.nbead * kPlLanes, T), T, 0, st>>>(s, koff);
+  else
+    k_pl<false><<<cdiv((long long)s.nbead * kPlLanes, T), T, 0, st>>>(s, koff);
 }
 
 }  // namespace sop

@@ -50,7 +50,7 @@ struct MolGrid {
   int base;                     // first global cell index
   int ncell;
   int brute;                    // 1: index-chunked cells, all pairs scanned
-  int pad;
+  int wrap;                     // 0: no pair of the molecule can reach boxl/4 (no minimum image)
 };
 
 struct DevSys {

@@ -137,6 +137,10 @@ def lib() -> ctypes.CDLL:
             "sop_serve_result": (I, [V, I, V, V, V, ctypes.POINTER(I), PLL,
                                      ctypes.POINTER(ctypes.c_double)]),
             "sop_serve_stats": (I, [V, V]),
+            "sop_checkpoint": (I, [V, I, V, LL, PLL]),
+            "sop_restore": (I, [V, I, V, LL]),
+            "sop_serve_checkpoint": (I, [V, I, V, LL, PLL]),
+            "sop_serve_resume": (I, [V, ctypes.POINTER(MoleculeDesc), V, LL, ctypes.POINTER(I)]),
             "sop_energy_noalloc": (I, [ctypes.POINTER(Params), ctypes.POINTER(EnergyLists), V, V]),
             "sop_energy_noalloc_error": (ctypes.c_char_p, []),
         }
@@ -305,6 +309,18 @@ class Engine:
         self._check(lib().sop_energy(self.h, mol, _p(t)), self.h)
         return t
 
+    def checkpoint(self, mol: int = 0) -> bytes:
+        """Exact checkpoint of a molecule (sop_checkpoint)."""
+        size = ctypes.c_longlong()
+        self._check(lib().sop_checkpoint(self.h, mol, None, 0, ctypes.byref(size)), self.h)
+        buf = ctypes.create_string_buffer(size.value)
+        self._check(lib().sop_checkpoint(self.h, mol, buf, size.value, ctypes.byref(size)), self.h)
+        return buf.raw[:size.value]
+
+    def restore(self, mol: int, blob: bytes) -> None:
+        """Continue molecule `mol` from a checkpoint (sop_restore)."""
+        self._check(lib().sop_restore(self.h, mol, blob, len(blob)), self.h)
+
     def observables(self, mol: int = 0) -> dict:
         o = np.zeros(4, np.float64)
         self._check(lib().sop_observables(self.h, mol, _p(o)), self.h)
@@ -378,6 +394,25 @@ class Server:
 
     def advance(self, rounds: int = 1) -> None:
         self._check(lib().sop_serve_advance(self.h, int(rounds)))
+
+    def checkpoint(self, job: int) -> bytes:
+        """Exact checkpoint of a running job, between rounds (sop_serve_checkpoint)."""
+        size = ctypes.c_longlong()
+        self._check(lib().sop_serve_checkpoint(self.h, job, None, 0, ctypes.byref(size)))
+        buf = ctypes.create_string_buffer(size.value)
+        self._check(lib().sop_serve_checkpoint(self.h, job, buf, size.value, ctypes.byref(size)))
+        return buf.raw[:size.value]
+
+    def resume(self, mol: Molecule, blob: bytes, nsteps: int, T: float = 0.6, traj: int = 0) -> int:
+        """Queue a job that continues from a checkpoint (sop_serve_resume);
+        nsteps is the job's total step budget."""
+        keep = []
+        d = _describe(mol, None, T, traj, nsteps, keep)
+        job = ctypes.c_int()
+        self._check(lib().sop_serve_resume(self.h, ctypes.byref(d), blob, len(blob),
+                                           ctypes.byref(job)))
+        self.sizes[job.value] = mol.n
+        return job.value
 
     def finished(self) -> list[int]:
         out = np.zeros(4096, np.int32)
