@@ -127,3 +127,18 @@ def test_rcut_matches_reference_rounding():
     rc = np.float32(3.2 * np.float64(r0))
     assert O.lib().orc_rcut2(3.2, 0.0, r0) == np.float32(rc * rc)
     assert O.lib().orc_rcut2(0.0, 32.0, r0) == np.float32(1024.0)
+
+
+def test_reference_shim_compiles_against_reference_headers():
+    """The reference-side shim (the reference's device-side entry points over
+    the C ABI) compiles against the reference's own headers, where a
+    reference tree is present."""
+    import shutil
+    import subprocess
+    if shutil.which("nvcc") is None:
+        pytest.skip("nvcc not available")
+    script = os.path.join(ROOT, "sop_gb300", "shim", "check_shim.sh")
+    r = subprocess.run(["bash", script], capture_output=True, text=True)
+    if r.returncode == 3:
+        pytest.skip("no reference source tree here")
+    assert r.returncode == 0, r.stderr
