@@ -113,4 +113,30 @@ void ref_gasdev(int run_id, int count, double* out) {
   for (int k = 0; k < count; ++k) out[k] = generator.gasdev();
 }
 
+// Wrapped coordinates (the reference's pos array).
+void ref_set_pos(const float* p) {
+  for (int i = 0; i < nbead; ++i) {
+    pos[i].x = p[3 * i]; pos[i].y = p[3 * i + 1]; pos[i].z = p[3 * i + 2];
+  }
+}
+
+// The reference's output writers on the current state: trajectory frames
+// (record_traj), coordinate and velocity files (save_coords, save_vels),
+// io.cpp:261-381.
+void ref_write_outputs(const char* traj, const char* traj_unc, const char* coord,
+                       const char* unccoord, const char* vels) {
+  record_traj(const_cast<char*>(traj), const_cast<char*>(traj_unc));
+  save_coords(const_cast<char*>(coord), const_cast<char*>(unccoord));
+  save_vels(const_cast<char*>(vels));
+}
+
+// One line of the reference's progress file for step istep (the sprintf of
+// underdamped_ctrl, sop.cu:256-259) after the energies and observables
+// above; rna_etot as energy_eval forms it (energy.cu:75).
+void ref_update_line(double istep, char* out, int cap) {
+  rna_etot = e_bnd + e_ang_ss + e_vdw_rr;
+  snprintf(out, cap, "%.0lf %f %f %f %f %f %f %f %f %f %d %f", istep, T, kinT, e_bnd, e_ang_ss,
+           e_vdw_rr_att, e_vdw_rr_rep, e_vdw_rr, rna_etot, Q, contct_nat, rgsq);
+}
+
 }  // extern "C"

@@ -13,6 +13,10 @@ Fixtures:
                                (energy.cu:194-225, 278-307, 369-442) and
                                observables (sop.cu:528-611) on them, for the
                                factor-mode and absolute-mode lists
+  m128_out.{traj,traj_unc,coord,unccoord,vel}
+                               the reference's output writers (io.cpp:261-381)
+                               on that state (wrapped = unwrapped coordinates)
+  m128_update.txt              its progress line for step 1000 (sop.cu:256-259)
 
 Run from the repository root: python tests/golden/make_golden.py
 """
@@ -96,6 +100,18 @@ def main():
         fx[f"{mode}_energy"] = e
     ob = np.zeros(4)
     R.ref_observables(P(ob))
+    # output files and the progress line (the absolute-mode lists are the
+    # current ones)
+    R.ref_set_pos(P(x))
+    outs = [os.path.join(HERE, f"m128_out.{k}") for k in ("traj", "traj_unc", "coord", "unccoord", "vel")]
+    for o in outs:
+        if os.path.exists(o):
+            os.remove(o)
+    R.ref_write_outputs(*[o.encode() for o in outs])
+    line = ctypes.create_string_buffer(1024)
+    R.ref_update_line(ctypes.c_double(1000.0), line, 1024)
+    with open(os.path.join(HERE, "m128_update.txt"), "w") as f:
+        f.write(line.value.decode() + "\n")
     np.savez_compressed(os.path.join(HERE, "m128_energy.npz"), x=x, v=v, observables=ob,
                         coeff_att_11=np.float32(0.7), **fx)
     print("golden fixtures written to", HERE)

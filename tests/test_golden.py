@@ -103,3 +103,26 @@ def test_oracle_forces_are_the_energy_gradient():
         _, em = O.forces_f64(m, xm, att, ri, rj)
         fd = -(ep.sum() - em.sum()) / (float(xp[b, c]) - float(xm[b, c]))
         assert fd == pytest.approx(f[b, c], rel=2e-4, abs=2e-5), (b, c)
+
+
+def test_output_writers_match_reference_writers(tmp_path):
+    """record_traj / save_coords / save_vels and the progress line write the
+    reference's files character for character (fixtures from io.cpp:261-381
+    and sop.cu:256-259 on the same state)."""
+    from sop_gb300 import outputs
+    g = np.load(os.path.join(GOLD, "m128_energy.npz"))
+    x, v = g["x"], g["v"]
+    p = {k: str(tmp_path / f"out.{k}") for k in ("traj", "traj_unc", "coord", "unccoord", "vel")}
+    outputs.record_traj(p["traj"], p["traj_unc"], x, x)
+    outputs.save_coords(p["coord"], p["unccoord"], x, x)
+    outputs.save_vels(p["vel"], v)
+    for k, path in p.items():
+        with open(path) as a, open(os.path.join(GOLD, f"m128_out.{k}")) as b:
+            assert a.read() == b.read(), k
+    pos, unc = outputs.load_coords(p["coord"], p["unccoord"], len(x))
+    np.testing.assert_allclose(unc, x, atol=5e-7)
+    e = g["absolute_energy"]
+    Q, rgsq, kinT, contct = g["observables"]
+    line = outputs.update_line(1000, 0.6, kinT, [e[0], e[1], e[2], e[3], 0.0], Q, int(contct), rgsq)
+    with open(os.path.join(GOLD, "m128_update.txt")) as f:
+        assert line == f.read().strip()
