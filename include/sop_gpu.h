@@ -77,6 +77,9 @@ typedef struct sop_params {
   int graph_steps;    /* steps per captured CUDA graph (0: the engine's default) */
   int lanes_per_bead; /* 0: autotuned table; else 1,2,4,8,16 or 32 */
   unsigned long long seed; /* Philox key (replaces setup_rng's seed, GPUvars.cu:417-453) */
+  int integrator;     /* 0: underdamped Langevin (sop.cu:421-462); 1: overdamped,
+                         x += (h / zeta) f with f = F + noise (sop.cu:487-521,
+                         a5 = h / zeta, param.cpp:110); velocities stay zero */
 } sop_params;
 
 /* Fills *p with the reference's defaults and the factor-mode list cut-offs. */

@@ -452,6 +452,15 @@ MolConst make_const(const sop_params& P, const HostMol& hm) {
   c.a2 = (float)(h * halfh);
   c.a3 = (float)((1.0 - h * z / 2.0 + (h * z) * (h * z) / 4.0) / h);
   c.a4 = (float)(halfh * (1.0 - h * z / 2.0));
+  if (P.integrator == 1) {
+    // overdamped: incr = a5 f (sop.cu:495-497), a5 = h / zeta (param.cpp:110).
+    // The step kernel's incr = fma(a1, v, a2 f) with a1 = 0 and a zero
+    // velocity is exactly that product, and v = a3 incr + a4 f stays 0.
+    c.a1 = 0.0f;
+    c.a2 = (float)(h / z);
+    c.a3 = 0.0f;
+    c.a4 = 0.0f;
+  }
   c.sigma_f = (float)std::sqrt(2.0 * T * z / h);
   c.t_zero = T < 1.0e-5 ? 1 : 0;
   c.traj = hm.traj;
@@ -815,12 +824,14 @@ void sop_params_default(sop_params* p) {
   p->graph_steps = 0;
   p->lanes_per_bead = 0;
   p->seed = 1234;       // setup_rng(1234, 0), sop.cu:138
+  p->integrator = 0;    // underdamped (param.cpp:249-253 selects)
 }
 
 int sop_ctx_create(const sop_params* p, void** out) {
   if (!p || !out) return SOP_ERR_ARG;
   *out = nullptr;
-  if (p->boxl <= 0 || p->h <= 0 || p->R0 <= 0 || p->graph_steps < 0) {
+  if (p->boxl <= 0 || p->h <= 0 || p->R0 <= 0 || p->graph_steps < 0 || p->integrator < 0 ||
+      p->integrator > 1 || (p->integrator == 1 && p->zeta <= 0)) {
     g_lib_error = "invalid parameters";
     return SOP_ERR_ARG;
   }

@@ -50,7 +50,8 @@ class Params(ctypes.Structure):
                 ("pl_rep_fac", ctypes.c_double), ("pl_rep_abs", ctypes.c_double),
                 ("nnlup", ctypes.c_int), ("nplup", ctypes.c_int), ("rep6", ctypes.c_int),
                 ("device", ctypes.c_int), ("graph_steps", ctypes.c_int),
-                ("lanes_per_bead", ctypes.c_int), ("seed", ctypes.c_ulonglong)]
+                ("lanes_per_bead", ctypes.c_int), ("seed", ctypes.c_ulonglong),
+                ("integrator", ctypes.c_int)]
 
 
 class MoleculeDesc(ctypes.Structure):

@@ -340,3 +340,31 @@ def test_long_run_stays_folded():
     assert np.all(np.isfinite(en))
     assert ob["Q"] > 0.6
     assert 0.2 < ob["kinT"] < 1.2
+
+
+def test_overdamped_steps_with_injected_noise():
+    """integrator = 1: x += (h / zeta) (F + sigma z) (sop.cu:487-521,
+    a5 = h / zeta), against FP64 forces on the same lists; velocities stay 0."""
+    mol = mol_of(128, 0)
+    x0 = perturbed(mol, 0.2, 1)
+    rng = np.random.default_rng(5)
+    z = rng.normal(0, 1, x0.shape).astype(np.float32)
+    T, h, zeta = 0.6, 0.001, 0.05
+    p = engine.baseline_params(integrator=1, h=h, zeta=zeta)
+    with engine.plain(mol, x0, p, T=T) as e:
+        e.set_noise(z)
+        e.force_eval()
+        e.step(3)
+        st = e.download()
+        assert e.status(0) == (0, 3)
+        pai, paj, _ = e.list_pairs(0, 2)
+        pri, prj, _ = e.list_pairs(0, 3)
+        assert e.observables()["kinT"] == 0.0
+    a5, sig = h / zeta, np.sqrt(2.0 * T * zeta / h)
+    x = x0.astype(np.float64)
+    sel = att_sel(mol, pai, paj)
+    for _ in range(3):   # no list rebuild within the first 10 steps
+        f, _ = O.forces_f64(mol, x.astype(np.float32), sel, pri, prj)
+        x = x + a5 * (f + sig * z)
+    np.testing.assert_allclose(st["unc_pos"], x, atol=5e-5)
+    assert np.all(st["vel"] == 0.0)
