@@ -2,7 +2,6 @@
 
   sop_gb300/libsopgpu.so   CUDA kernels + C ABI (include/sop_gpu.h), sm_103a
   sop_gb300/libsopgen.so   synthetic structure generator (host C++)
-  sop_gb300/sop2_gb300     drop-in driver for the reference's input scripts
 
 Translation units compile in parallel; one -gencode (compute_103a / sm_103a).
 """
