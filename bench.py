@@ -139,6 +139,24 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(x: float, world: int, device) -> float:
+    """The largest x over the ranks (the slowest rank's time); x itself on
+    one rank."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(beads_per_rank: int, md_steps: int, world: int, t_max: float) -> float:
+    """Bead-steps/s of the whole job: every rank runs its own replica of the
+    workload (weak scaling), timed by the slowest rank."""
+    return world * beads_per_rank * md_steps / t_max
+
+
 def launches_per_bench_step(p, s0: int) -> int:
     """Kernels of the engine in one replay starting after step s0."""
     nl_kernels = 11    # bbox reset, bbox, grid, grid base, assign, 3 scan, scatter, cellsort, nl
@@ -502,12 +520,8 @@ def main() -> None:
         raise RuntimeError("a neighbour-list overflow re-ran steps outside the timed region")
     statuses = [e.status(m)[0] for m in range(len(mols))]
     t_local = sum(ms) / 1e3
-    t_max = t_local
-    if world > 1:
-        tt = torch.tensor([t_local], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = world * total * MD_STEPS * K / t_max
+    t_max = max_over_ranks(t_local, world, dev)
+    value = whole_job_rate(total, MD_STEPS * K, world, t_max)
 
     # ---- roofline of the dominant kernel (the fused step kernel), timed alone
     byts, ls = step_kernel_bytes(e, mols)
@@ -547,11 +561,8 @@ def main() -> None:
         dt = time.perf_counter() - t0
         e2.close()
         barrier()
-        if world > 1:
-            tt = torch.tensor([dt], device=dev, dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            dt = float(tt.item())
-        e2e = {"value": world * total * MD_STEPS * K2 / dt, "unit": UNIT,
+        dt = max_over_ranks(dt, world, dev)
+        e2e = {"value": whole_job_rate(total, MD_STEPS * K2, world, dt), "unit": UNIT,
                "h2d_bytes_per_step": int(h2d / K2), "d2h_bytes_per_step": int(12 * total),
                "steps": K2, "note": "wall clock: context creation, upload of every structure from "
                                      "host arrays, set-up, then per step 10 Langevin steps and a "
