@@ -434,6 +434,8 @@ __global__ void __launch_bounds__(256) k_nl(DevSys s) {
 constexpr int kPlLanes = 8;   // lanes per bead in the pair-list rebuild
 template <bool UNI>
 __global__ void __launch_bounds__(256) k_pl(DevSys s, int koff) {
+  pdl_wait();
+  pdl_release();
   const int wl = threadIdx.x & 31;
   const int lane = wl & (kPlLanes - 1);
   const unsigned gmask = ((1u << kPlLanes) - 1u) << (wl & ~(kPlLanes - 1));
@@ -568,9 +570,9 @@ void launch_rebin(const DevSys& s, const NLScratch& w, cudaStream_t st) {
 void launch_pl_rebuild(const DevSys& s, int koff, cudaStream_t st) {
   const int T = 256;
   if (s.uniform_type)
-    k_pl<true><<<cdiv((long long)s.nbead * kPlLanes, T), T, 0, st>>>(s, koff);
+    launch_pdl(k_pl<true>, cdiv((long long)s.nbead * kPlLanes, T), T, st, s, koff);
   else
-    k_pl<false><<<cdiv((long long)s.nbead * kPlLanes, T), T, 0, st>>>(s, koff);
+    launch_pdl(k_pl<false>, cdiv((long long)s.nbead * kPlLanes, T), T, st, s, koff);
 }
 
 }  // namespace sop

@@ -88,6 +88,8 @@ __device__ __forceinline__ float small_coeff(const DevSys& s, int type, float dx
 template <int G, bool STEP, bool UNI>
 __global__ void __launch_bounds__(256, StepBlocks<G>::value) k_step(DevSys s, int koff) {
   constexpr int BPB = 256 / G;          // beads per block
+  pdl_wait();
+  pdl_release();
   __shared__ float4 fsum[BPB];          // conservative force sums; w = FENE range flag
   __shared__ int bead[BPB];             // bead of each slot, -1: nothing to do
   const int slot = threadIdx.x / G;
@@ -286,6 +288,8 @@ __global__ void __launch_bounds__(256, StepBlocks<G>::value) k_step(DevSys s, in
 // count (clamped to its budget).  A neighbour-list overflow freezes
 // everything until the host regrows the list and re-runs the block.
 __global__ void k_advance(DevSys s, int steps) {
+  pdl_wait();
+  pdl_release();
   int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (*s.flags & FLAG_NL_OVERFLOW) return;
   if (m == 0) *s.sys_step += steps;  // the context's clock (blocks completed)
@@ -462,11 +466,11 @@ template <int G>
 static void launch_step_g(const DevSys& s, int koff, bool step, cudaStream_t st) {
   const unsigned blocks = cdiv(s.nbead, 256 / G);
   if (s.uniform_type) {
-    if (step) k_step<G, true, true><<<blocks, 256, 0, st>>>(s, koff);
-    else k_step<G, false, true><<<blocks, 256, 0, st>>>(s, koff);
+    if (step) launch_pdl(k_step<G, true, true>, blocks, 256, st, s, koff);
+    else launch_pdl(k_step<G, false, true>, blocks, 256, st, s, koff);
   } else {
-    if (step) k_step<G, true, false><<<blocks, 256, 0, st>>>(s, koff);
-    else k_step<G, false, false><<<blocks, 256, 0, st>>>(s, koff);
+    if (step) launch_pdl(k_step<G, true, false>, blocks, 256, st, s, koff);
+    else launch_pdl(k_step<G, false, false>, blocks, 256, st, s, koff);
   }
 }
 
@@ -485,7 +489,7 @@ void launch_gather_current(const DevSys& s, float4* out, cudaStream_t st) {
 }
 
 void launch_advance(const DevSys& s, int steps, cudaStream_t st) {
-  k_advance<<<cdiv(s.nmol, 256), 256, 0, st>>>(s, steps);
+  launch_pdl(k_advance, cdiv(s.nmol, 256), 256, st, s, steps);
 }
 
 void launch_energy(const DevSys& s, int mol_start, int mol_n, int m, double* part, double* out,

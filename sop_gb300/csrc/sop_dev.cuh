@@ -104,6 +104,34 @@ struct DevSys {
 enum { FLAG_NL_OVERFLOW = 1 };
 
 // --------------------------------------------------------------- helpers
+// Programmatic dependent launch.  The per-step kernels are launched with
+// programmatic stream serialisation, so the next one's blocks may be
+// scheduled while the previous kernel's last wave drains.  pdl_wait() blocks
+// until the previous kernel on the stream has completed and its writes are
+// visible (a no-op after an ordinary launch); pdl_release() lets the next
+// kernel be scheduled.  Each such kernel waits before its first global access,
+// so completion is transitive along the chain.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launch with programmatic stream serialisation (see pdl_wait).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), unsigned grid, unsigned block,
+                              cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
 __device__ __forceinline__ int type_of(float4 a) { return __float_as_int(a.w); }
 
 // Entry (ti, tj) of a symmetric per-type-pair table (types are 1 or 2),
