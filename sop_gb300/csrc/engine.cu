@@ -596,9 +596,43 @@ int alloc_pools(SopCtx* ctx, const Caps& c) {
 // the pools, rows with absolute offsets, x_0 in both coordinate buffers, its
 // lists empty, and mol_step = step0 (0: starts now; < 0: starts -step0 steps
 // into the next block sequence).  Returns SOP_ERR_CAPACITY if a pool is full.
-int install(SopCtx* ctx, int slot, HostMol& hm, long long step0) {
+// Host copies of the device rows of one or more molecules installed in
+// consecutive pool ranges (beads [o, o + n), bond / angle / native entries
+// from ob / oa / on, molecule slots from slot0), uploaded with one copy per
+// array.
+struct Staged {
+  long long o = 0, ob = 0, oa = 0, on = 0;
+  int slot0 = 0;
+  std::vector<int2> brow, arow, nrow;
+  std::vector<int> bj, aj, nj, molof;
+  std::vector<float> br;
+  std::vector<float4> np, x0, p0, v0;
+  std::vector<float2> nr;
+  std::vector<long long> step0;
+  std::vector<MolConst> mc;
+  long long beads() const { return (long long)x0.size(); }
+  // appends `t` if its ranges follow on from these; false otherwise
+  bool append(Staged& t) {
+    if (mc.empty()) {
+      *this = std::move(t);
+      return true;
+    }
+    if (t.o != o + beads() || t.ob != ob + (long long)bj.size() || t.oa != oa + (long long)aj.size() ||
+        t.on != on + (long long)nj.size() || t.slot0 != slot0 + (int)mc.size())
+      return false;
+    auto cat = [](auto& a, auto& b) { a.insert(a.end(), b.begin(), b.end()); };
+    cat(brow, t.brow); cat(arow, t.arow); cat(nrow, t.nrow);
+    cat(bj, t.bj); cat(aj, t.aj); cat(nj, t.nj); cat(molof, t.molof);
+    cat(br, t.br); cat(np, t.np); cat(x0, t.x0); cat(p0, t.p0); cat(v0, t.v0);
+    cat(nr, t.nr); cat(step0, t.step0); cat(mc, t.mc);
+    return true;
+  }
+};
+
+// Takes pool ranges for molecule `hm` in slot `slot` and builds its device
+// rows on the host.  SOP_ERR_CAPACITY when the pools cannot hold it.
+int stage_install(SopCtx* ctx, int slot, HostMol& hm, long long step0, Staged& S) {
   const sop_params& P = ctx->P;
-  DevSys& s = ctx->s;
   const long long nb2 = 2LL * (long long)hm.bi.size(), na2 = 2LL * (long long)hm.ai.size(),
                   nn2 = 2LL * (long long)hm.ni.size();
   long long b0 = ctx->bead_alloc.alloc(hm.n);
@@ -617,7 +651,8 @@ int install(SopCtx* ctx, int slot, HostMol& hm, long long step0) {
   hm.slot = slot;
   hm.off_b = ob; hm.off_a = oa; hm.off_n = on;
   const int n = hm.n, o = (int)b0;
-  std::vector<int2> brow(n), arow(n), nrow(n);
+  S.o = b0; S.ob = ob; S.oa = oa; S.on = on; S.slot0 = slot;
+  S.brow.assign(n, int2{}); S.arow.assign(n, int2{}); S.nrow.assign(n, int2{});
   std::vector<int> cnt_b(n, 0), cnt_a(n, 0), cnt_n(n, 0);
   for (size_t k = 0; k < hm.bi.size(); ++k) { cnt_b[hm.bi[k]]++; cnt_b[hm.bj[k]]++; }
   for (size_t k = 0; k < hm.ai.size(); ++k) { cnt_a[hm.ai[k]]++; cnt_a[hm.ak[k]]++; }
@@ -625,26 +660,26 @@ int install(SopCtx* ctx, int slot, HostMol& hm, long long step0) {
   {
     int eb = (int)ob, ea = (int)oa, en = (int)on;
     for (int i = 0; i < n; ++i) {
-      brow[i] = make_int2(eb, 0); eb += cnt_b[i];
-      arow[i] = make_int2(ea, 0); ea += cnt_a[i];
-      nrow[i] = make_int2(en, 0); en += cnt_n[i];
+      S.brow[i] = make_int2(eb, 0); eb += cnt_b[i];
+      S.arow[i] = make_int2(ea, 0); ea += cnt_a[i];
+      S.nrow[i] = make_int2(en, 0); en += cnt_n[i];
     }
   }
-  std::vector<int> bj(nb2), aj(na2), nj(nn2), molof(n, slot);
-  std::vector<float> br(nb2);
-  std::vector<float4> np(nn2);
-  std::vector<float2> nr(nn2);
+  S.bj.assign(nb2, 0); S.aj.assign(na2, 0); S.nj.assign(nn2, 0); S.molof.assign(n, slot);
+  S.br.assign(nb2, 0.f);
+  S.np.assign(nn2, float4{});
+  S.nr.assign(nn2, float2{});
   auto put_b = [&](int i, int j, float r0) {
-    int e = brow[i].x + brow[i].y++ - (int)ob;
-    bj[e] = o + j; br[e] = r0;
+    int e = S.brow[i].x + S.brow[i].y++ - (int)ob;
+    S.bj[e] = o + j; S.br[e] = r0;
   };
-  auto put_a = [&](int i, int j) { aj[arow[i].x + arow[i].y++ - (int)oa] = o + j; };
+  auto put_a = [&](int i, int j) { S.aj[S.arow[i].x + S.arow[i].y++ - (int)oa] = o + j; };
   auto put_n = [&](int i, int j, float r0, float ef, float ee) {
-    int e = nrow[i].x + nrow[i].y++ - (int)on;
-    nj[e] = o + j;
-    np[e] = make_float4(r0, ef, ee, 0.f);
-    nr[e] = make_float2(rcut2_of(P.nl_att_fac, P.nl_att_abs, r0),
-                        rcut2_of(P.pl_att_fac, P.pl_att_abs, r0));
+    int e = S.nrow[i].x + S.nrow[i].y++ - (int)on;
+    S.nj[e] = o + j;
+    S.np[e] = make_float4(r0, ef, ee, 0.f);
+    S.nr[e] = make_float2(rcut2_of(P.nl_att_fac, P.nl_att_abs, r0),
+                          rcut2_of(P.pl_att_fac, P.pl_att_abs, r0));
   };
   for (size_t k = 0; k < hm.bi.size(); ++k) {
     put_b(hm.bi[k], hm.bj[k], hm.br0[k]);
@@ -658,49 +693,67 @@ int install(SopCtx* ctx, int slot, HostMol& hm, long long step0) {
     put_n(hm.ni[k], hm.nj[k], hm.nr0[k], hm.neps[k], hm.nepse[k]);
     put_n(hm.nj[k], hm.ni[k], hm.nr0[k], hm.neps[k], hm.nepse[k]);
   }
-  std::vector<float4> x0(n), p0(n), v0(n);
+  S.x0.assign(n, float4{}); S.p0.assign(n, float4{}); S.v0.assign(n, float4{});
   for (int i = 0; i < n; ++i) {
     int t = hm.types.empty() ? 1 : hm.types[i];
-    x0[i] = make_float4(hm.unc[3 * i], hm.unc[3 * i + 1], hm.unc[3 * i + 2], bits_f(t));
+    S.x0[i] = make_float4(hm.unc[3 * i], hm.unc[3 * i + 1], hm.unc[3 * i + 2], bits_f(t));
     const std::vector<float>& pp = hm.pos.empty() ? hm.unc : hm.pos;
-    p0[i] = make_float4(pp[3 * i], pp[3 * i + 1], pp[3 * i + 2], 0.f);
-    v0[i] = hm.vel.empty() ? make_float4(0.f, 0.f, 0.f, 0.f)
-                           : make_float4(hm.vel[3 * i], hm.vel[3 * i + 1], hm.vel[3 * i + 2], 0.f);
+    S.p0[i] = make_float4(pp[3 * i], pp[3 * i + 1], pp[3 * i + 2], 0.f);
+    S.v0[i] = hm.vel.empty() ? make_float4(0.f, 0.f, 0.f, 0.f)
+                             : make_float4(hm.vel[3 * i], hm.vel[3 * i + 1], hm.vel[3 * i + 2], 0.f);
   }
   MolConst mcst = make_const(P, hm);
   ctx->mc[slot] = mcst;
+  S.mc.assign(1, mcst);
+  S.step0.assign(1, step0);
+  return SOP_OK;
+}
+
+// Uploads staged rows (one copy per array) and waits for the copies.
+int upload_staged(SopCtx* ctx, const Staged& S) {
+  if (S.mc.empty()) return SOP_OK;
+  DevSys& s = ctx->s;
   cudaStream_t st = ctx->stream;
-  const size_t f4 = sizeof(float4) * n;
+  const long long n = S.beads(), o = S.o;
+  const size_t f4 = sizeof(float4) * (size_t)n;
+  auto up = [&](auto* dst, const auto& v) -> cudaError_t {
+    if (v.empty()) return cudaSuccess;
+    return cudaMemcpyAsync(dst, v.data(), sizeof(v[0]) * v.size(), cudaMemcpyHostToDevice, st);
+  };
   for (int b = 0; b < 2; ++b) {
-    CK(cudaMemcpyAsync(s.x[b] + o, x0.data(), f4, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(s.p[b] + o, p0.data(), f4, cudaMemcpyHostToDevice, st));
+    CK(up(s.x[b] + o, S.x0));
+    CK(up(s.p[b] + o, S.p0));
   }
-  CK(cudaMemcpyAsync(s.v + o, v0.data(), f4, cudaMemcpyHostToDevice, st));
+  CK(up(s.v + o, S.v0));
   CK(cudaMemsetAsync(s.incr + o, 0, f4, st));
   CK(cudaMemsetAsync(s.f + o, 0, f4, st));
-  CK(cudaMemcpyAsync(s.bond_row + o, brow.data(), sizeof(int2) * n, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(s.ang_row + o, arow.data(), sizeof(int2) * n, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(s.nat_row + o, nrow.data(), sizeof(int2) * n, cudaMemcpyHostToDevice, st));
-  if (nb2) {
-    CK(cudaMemcpyAsync(s.bond_j + ob, bj.data(), sizeof(int) * nb2, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(s.bond_r0 + ob, br.data(), sizeof(float) * nb2, cudaMemcpyHostToDevice, st));
-  }
-  if (na2) CK(cudaMemcpyAsync(s.ang_j + oa, aj.data(), sizeof(int) * na2, cudaMemcpyHostToDevice, st));
-  if (nn2) {
-    CK(cudaMemcpyAsync(s.nat_j + on, nj.data(), sizeof(int) * nn2, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(s.nat_par + on, np.data(), sizeof(float4) * nn2, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(s.nat_rc2 + on, nr.data(), sizeof(float2) * nn2, cudaMemcpyHostToDevice, st));
-  }
-  CK(cudaMemsetAsync(s.nl_cnt + o, 0, sizeof(int) * n, st));
-  CK(cudaMemsetAsync(s.pl_cnt + o, 0, sizeof(int) * n, st));
-  CK(cudaMemsetAsync(s.nl_att_cnt + o, 0, sizeof(int) * n, st));
-  CK(cudaMemsetAsync(s.pl_att_cnt + o, 0, sizeof(int) * n, st));
-  CK(cudaStreamSynchronize(st));  // the host vectors above go out of scope
-  CK(cudaMemcpy(s.mol_step + slot, &step0, sizeof(long long), cudaMemcpyHostToDevice));
-  CK(cudaMemset(s.mol_status + slot, 0, sizeof(int)));
-  CK(cudaMemcpy(s.mol_of + o, molof.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(ctx->dmol + slot, &mcst, sizeof(MolConst), cudaMemcpyHostToDevice));
+  CK(up(s.bond_row + o, S.brow));
+  CK(up(s.ang_row + o, S.arow));
+  CK(up(s.nat_row + o, S.nrow));
+  CK(up(s.bond_j + S.ob, S.bj));
+  CK(up(s.bond_r0 + S.ob, S.br));
+  CK(up(s.ang_j + S.oa, S.aj));
+  CK(up(s.nat_j + S.on, S.nj));
+  CK(up(s.nat_par + S.on, S.np));
+  CK(up(s.nat_rc2 + S.on, S.nr));
+  CK(cudaMemsetAsync(s.nl_cnt + o, 0, sizeof(int) * (size_t)n, st));
+  CK(cudaMemsetAsync(s.pl_cnt + o, 0, sizeof(int) * (size_t)n, st));
+  CK(cudaMemsetAsync(s.nl_att_cnt + o, 0, sizeof(int) * (size_t)n, st));
+  CK(cudaMemsetAsync(s.pl_att_cnt + o, 0, sizeof(int) * (size_t)n, st));
+  CK(up(s.mol_step + S.slot0, S.step0));
+  CK(cudaMemsetAsync(s.mol_status + S.slot0, 0, sizeof(int) * S.mc.size(), st));
+  CK(up(s.mol_of + o, S.molof));
+  CK(up(ctx->dmol + S.slot0, S.mc));
+  CK(cudaStreamSynchronize(st));  // the host arrays may go out of scope
   return SOP_OK;
+}
+
+// One molecule into slot `slot`, its step counter at step0.
+int install(SopCtx* ctx, int slot, HostMol& hm, long long step0) {
+  Staged S;
+  int rc = stage_install(ctx, slot, hm, step0, S);
+  if (rc) return rc;
+  return upload_staged(ctx, S);
 }
 
 // Frees molecule slot `slot`: inactive on the device, its beads unowned,
@@ -763,11 +816,22 @@ int commit(SopCtx* ctx) {
   for (auto& m : ctx->mols)
     for (int t : m.types)
       if (t != 1) ctx->s.uniform_type = 0;
+  // every molecule's rows staged on the host, then one copy per array (the
+  // pools are fresh, so the molecules' ranges follow one another)
+  Staged all;
   for (int k = 0; k < (int)ctx->mols.size(); ++k) {
     ctx->free_slots.pop_back();  // slots handed out in id order
-    rc = install(ctx, k, ctx->mols[k], 0);
+    Staged one;
+    rc = stage_install(ctx, k, ctx->mols[k], 0, one);
     if (rc) return ctx->fail(rc, "pool sizing error");
+    if (!all.append(one)) {
+      rc = upload_staged(ctx, all);
+      if (rc) return rc;
+      all = std::move(one);
+    }
   }
+  rc = upload_staged(ctx, all);
+  if (rc) return rc;
   rc = setup_step0(ctx);
   if (rc) return rc;
   ctx->host_step = 0;
