@@ -37,7 +37,7 @@ long long scan_block_sums_needed(long long n);
 // kernels_step.cu
 void launch_step(const DevSys& s, int G, int koff, bool step, cudaStream_t st);
 void launch_advance(const DevSys& s, int steps, cudaStream_t st);
-void launch_gather_current(const DevSys& s, float4* out, cudaStream_t st);
+void launch_gather_current(const DevSys& s, float* out, cudaStream_t st);
 void launch_energy(const DevSys& s, int mol_start, int mol_n, int m, double* part, double* out,
                    double k_bnd_R0sq_half, cudaStream_t st);
 void launch_observables(const DevSys& s, int mol_start, int mol_n, int m, int nnat,
@@ -1732,10 +1732,12 @@ int sop_download_all(void* p, float* unc_pos) {
     ctx->stage = ctx->dalloc<float4>(ctx->s.nbead);
     if (!ctx->stage) return ctx->fail(SOP_ERR_ALLOC, "staging buffer allocation failed");
   }
-  launch_gather_current(ctx->s, ctx->stage, ctx->stream);
+  // the staging buffer (nbead float4) holds the packed 3 * nbead floats
+  float* packed = reinterpret_cast<float*>(ctx->stage);
+  launch_gather_current(ctx->s, packed, ctx->stream);
   CK(cudaGetLastError());
-  rc = copy3(ctx, unc_pos, ctx->stage, ctx->s.nbead);
-  if (rc) return rc;
+  CK(cudaMemcpyAsync(unc_pos, packed, sizeof(float) * 3 * (size_t)ctx->s.nbead,
+                     cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return SOP_OK;
 }

@@ -322,6 +322,13 @@ constexpr int kNatRegs = 16;  // native partners held in registers (the rest are
 constexpr int kNlLanes = 8;
 
 // Distance from v to the slab [a, a + w] (0 inside).
+// cell_coord with a multiply by the inverse edge: for bounds that carry a
+// margin far above its rounding (about 1e-5 cells)
+__device__ __forceinline__ int cell_coord_fast(float v, float lo, float inv_cs, int dim) {
+  int c = (int)floorf((v - lo) * inv_cs);
+  return c < 0 ? 0 : (c >= dim ? dim - 1 : c);
+}
+
 __device__ __forceinline__ float slab_dist(float v, float a, float w) {
   return fmaxf(fmaxf(a - v, v - (a + w)), 0.0f);
 }
@@ -358,6 +365,7 @@ __global__ void __launch_bounds__(256) k_nl(DevSys s) {
   const int x0 = max(cx - g.S, 0), x1 = min(cx + g.S, nx - 1);
   const float boxl = s.boxl;
   const bool wrap = g.wrap != 0;
+  const float inv_cs = g.brute ? 0.0f : 1.0f / g.cs;
   const float r11 = s.rc2_nl_rep[1][1], r12 = s.rc2_nl_rep[1][2], r22 = s.rc2_nl_rep[2][2];
   const float rcm = s.rc_nl_rep_max * 1.0001f + 1.0e-3f;
   const float rcm2 = rcm * rcm;
@@ -377,9 +385,12 @@ __global__ void __launch_bounds__(256) k_nl(DevSys s) {
       if (rem < 0.0f) continue;
       int xa = x0, xb = x1;
       if (!g.brute) {
-        const float w = sqrtf(rem);
-        xa = max(x0, cell_coord(xi.x - w, g.lo[0], g.cs, nx));
-        xb = min(x1, cell_coord(xi.x + w, g.lo[0], g.cs, nx));
+        // the chord only bounds the candidates (the exact predicate decides):
+        // an approximate root and reciprocal, widened by 1e-3 A, keep it a
+        // superset at a fraction of the cost of the exact operations
+        const float w = __fmul_rn(rem, rsqrtf(fmaxf(rem, 1.0e-30f))) * 1.0001f + 1.0e-3f;
+        xa = max(x0, cell_coord_fast(xi.x - w, g.lo[0], inv_cs, nx));
+        xb = min(x1, cell_coord_fast(xi.x + w, g.lo[0], inv_cs, nx));
       }
       const int rowc = g.base + (z * ny + y) * nx;
       const int ja = s.cell_start[rowc + xa];

@@ -452,11 +452,14 @@ __global__ void k_observables_final(const double* __restrict__ part, int nblocks
 
 // Every bead's current unwrapped coordinates (each molecule at its own step
 // parity) in bead-id order, for one device-to-host copy.
-__global__ void k_gather_current(DevSys s, float4* __restrict__ out) {
+__global__ void k_gather_current(DevSys s, float* __restrict__ out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= s.nbead) return;
   int m = s.mol_of[i];
-  out[i] = m < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : s.x[(int)(s.mol_step[m] & 1)][i];
+  const float4 x = m < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : s.x[(int)(s.mol_step[m] & 1)][i];
+  out[3 * (long long)i] = x.x;       // packed xyz: one contiguous copy to the host
+  out[3 * (long long)i + 1] = x.y;
+  out[3 * (long long)i + 2] = x.z;
 }
 
 // ----------------------------------------------------------- launchers
@@ -484,7 +487,7 @@ void launch_step(const DevSys& s, int G, int koff, bool step, cudaStream_t st) {
   }
 }
 
-void launch_gather_current(const DevSys& s, float4* out, cudaStream_t st) {
+void launch_gather_current(const DevSys& s, float* out, cudaStream_t st) {
   k_gather_current<<<cdiv(s.nbead, 256), 256, 0, st>>>(s, out);
 }
 

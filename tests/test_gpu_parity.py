@@ -368,3 +368,18 @@ def test_overdamped_steps_with_injected_noise():
         x = x + a5 * (f + sig * z)
     np.testing.assert_allclose(st["unc_pos"], x, atol=5e-5)
     assert np.all(st["vel"] == 0.0)
+
+
+def test_download_all_matches_per_molecule_downloads():
+    """sop_download_all: every molecule's current coordinates in id order,
+    the same as downloading them one by one."""
+    mols = [mol_of(128, 0), mol_of(4000, 1), mol_of(300, 5)]
+    e = engine.Engine(engine.baseline_params())
+    for k, m in enumerate(mols):
+        e.add(m, m.xyz, T=0.6, traj=k)
+    e.commit()
+    e.step(17)
+    allx = e.download_all()
+    each = np.concatenate([e.download(k)["unc_pos"] for k in range(len(mols))])
+    e.close()
+    np.testing.assert_array_equal(allx, each)
