@@ -449,6 +449,8 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-loop comparison")
     ap.add_argument("--no-served", action="store_true", help="skip the served request stream")
+    ap.add_argument("--lanes", type=int, default=0,
+                    help="lanes per bead of the step kernel (2, 4, 8, 16); 0: autotuned")
     ap.add_argument("--workload", default="ensemble", choices=["ensemble", *PLAIN],
                     help="ensemble: the batched ensemble (with the served stream beside it); "
                          "plain128 / plain4000 / plain50k: the plain path on one structure")
@@ -485,7 +487,7 @@ def main() -> None:
 
     mols, ts = ensemble(rank)
     total = sum(m.n for m in mols)
-    p = engine.baseline_params(device=local, graph_steps=MD_STEPS)
+    p = engine.baseline_params(device=local, graph_steps=MD_STEPS, lanes_per_bead=args.lanes)
     e = engine.Engine(p)
     for k, (m, t) in enumerate(zip(mols, ts)):
         e.add(m, m.xyz, T=float(t), traj=rank * N_TRAJ + k)
