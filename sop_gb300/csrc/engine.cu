@@ -1837,6 +1837,11 @@ int sop_restore(void* p, int mol, const void* buf, long long size) {
     return ctx->fail(SOP_ERR_ARG, "checkpoint step differs from the context's step");
   rc = restore_into(ctx, mol, static_cast<const char*>(buf), size);
   if (rc) return rc;
+  // refresh the cell order and each molecule's grid flags from the restored
+  // coordinates (binning only: no list changes, no result depends on it)
+  launch_rebin(ctx->s, ctx->w, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
   if (set_clock) {
     ctx->host_step = ctx->target_step = step;
     CK(cudaMemcpy(ctx->s.sys_step, &step, sizeof(long long), cudaMemcpyHostToDevice));

@@ -126,6 +126,10 @@ __global__ void __launch_bounds__(256, StepBlocks<G>::value) k_step(DevSys s, in
     const float4* __restrict__ X = s.x[(int)(n & 1)];
     const float4 xi = X[i];
     const float boxl = s.boxl;
+    // 0 when no pair of the molecule can reach boxl/4 (from its last binning,
+    // with a cut-off of margin): the minimum image is then the identity and
+    // its test is skipped
+    const bool wrap = s.grid[m1].wrap != 0;
     // Row descriptors first, as independent loads.
     const int2 br = s.bond_row[i];
     const int2 ar = s.ang_row[i];
@@ -163,7 +167,7 @@ __global__ void __launch_bounds__(256, StepBlocks<G>::value) k_step(DevSys s, in
         float lx, ly, lz;
         float dx = diff_exact(xj.x, xi.x, lx), dy = diff_exact(xj.y, xi.y, ly),
               dz = diff_exact(xj.z, xi.z, lz);
-        min_image3(dx, dy, dz, boxl);
+        if (wrap) min_image3(dx, dy, dz, boxl);
         const float cc = small_coeff(s, t, dx, dy, dz, lx, ly, lz, r0, eps, fene_bad);
         acc3(ax[c], ay[c], az[c], cc, dx, dy, dz);
       }
@@ -197,7 +201,7 @@ __global__ void __launch_bounds__(256, StepBlocks<G>::value) k_step(DevSys s, in
         float dx = __fsub_rn(xx[c].x, xi.x), dy = __fsub_rn(xx[c].y, xi.y),
               dz = __fsub_rn(xx[c].z, xi.z);
         // |dx| + |dy| + |dz| bounds every component: one test for the rare wrap
-        if (fabsf(dx) + fabsf(dy) + fabsf(dz) > q4) min_image3(dx, dy, dz, boxl);
+        if (wrap && fabsf(dx) + fabsf(dy) + fabsf(dz) > q4) min_image3(dx, dy, dz, boxl);
         const float d2 = d2_plain(dx, dy, dz);
         float sg2 = g11, tol = t11;
         if (!UNI) {
