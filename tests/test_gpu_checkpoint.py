@@ -118,3 +118,21 @@ def test_served_job_resumes_bit_identically():
     assert got["steps"] == 400 and got["status"] == ref["status"]
     for k in ("unc_pos", "vel", "energy"):
         np.testing.assert_array_equal(got[k], ref[k])
+
+
+def test_restore_into_a_context_built_from_other_coordinates():
+    """A checkpoint of a fully extended chain (15,200 A, past a quarter of its
+    40,000 A box, where the minimum image matters) restored into a context
+    committed from the compact native structure: the continuation is still
+    bit-identical (the restore refreshes the cell order and grid flags)."""
+    mol = mol_of(4000, 1)
+    p = engine.baseline_params(boxl=40000.0)
+    with engine.plain(mol, mol.extended_xyz(), p, T=0.6, traj=3) as e:
+        e.step(60)
+        blob = e.checkpoint(0)
+        e.step(90)
+        ref = state(e)
+    with engine.plain(mol, mol.xyz, p, T=0.6, traj=3) as e:
+        e.restore(0, blob)
+        e.step(90)
+        same(state(e), ref)
