@@ -157,15 +157,16 @@ def whole_job_rate(beads_per_rank: int, md_steps: int, world: int, t_max: float)
     return world * beads_per_rank * md_steps / t_max
 
 
-def launches_per_bench_step(p, s0: int) -> int:
-    """Kernels of the engine in one replay starting after step s0."""
+def launches_per_bench_step(p, s0: int, step_kernels: int = 1) -> int:
+    """Kernels of the engine in one replay starting after step s0
+    (step_kernels: 1 for the one-kernel step, 2 for force + finish)."""
     nl_kernels = 11    # bbox reset, bbox, grid, grid base, assign, 3 scan, scatter, cellsort, nl
     n = 0
     for k in range(MD_STEPS):
         st = s0 + 1 + k
         nl = p.nnlup > 0 and st % p.nnlup == 0
         pl = nl or p.nplup <= 1 or st % p.nplup == 0
-        n += (nl_kernels if nl else 0) + (1 if pl else 0) + 1
+        n += (nl_kernels if nl else 0) + (1 if pl else 0) + step_kernels
     return n + 1   # step advance
 
 
@@ -336,7 +337,8 @@ def plain_one(args, local: int) -> None:
         # cell binning (bbox, cells, sorted copy) + writing both directions of the NL
         2: 64.0 * N + 8.0 * ls["nnl_rep"] + 8.0 * ls["nnl_att"],
     }
-    names = {0: "fused force + Langevin step (k_step)", 1: "pair-list rebuild (k_pl)",
+    names = {0: "force + Langevin step (k_step; + k_finish in the two-kernel form)",
+             1: "pair-list rebuild (k_pl)",
              2: "neighbour-list rebuild (binning + k_nl)"}
     stages = {}
     for st in (0, 1, 2):
@@ -355,9 +357,10 @@ def plain_one(args, local: int) -> None:
         stages[names[st]] = {"us": tk * 1e6, "bytes": stage_bytes[st], "achieved_gbs": ach,
                              "frac": ach / peak}
     e.sync()
+    tuning = e.tuning()
     e.close()
     s0 = stages[names[0]]
-    n_launch = sum(launches_per_bench_step(p, k * MD_STEPS) for k in range(K))
+    n_launch = sum(launches_per_bench_step(p, k * MD_STEPS, tuning["form"]) for k in range(K))
     cpu = None
     if not args.no_cpu_baseline:
         # the reference algorithm on one host core, in whole neighbour-list
@@ -389,7 +392,7 @@ def plain_one(args, local: int) -> None:
             "roofline": {"bound": "hbm", "achieved": s0["achieved_gbs"], "peak": peak,
                          "unit": "GB/s", "frac": s0["frac"], "traffic": None,
                          "kernel": names[0], "peak_source": peak_kind},
-            "cpu_baseline": cpu,
+            "cpu_baseline": cpu, "tuning": tuning,
             "stages": stages, "lists": ls, "gpu_launches": int(n_launch), "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 
@@ -599,7 +602,8 @@ def main() -> None:
         served = served_stream(local)
 
     if rank == 0:
-        n_launch = sum(launches_per_bench_step(p, s_start + k * MD_STEPS) for k in range(K))
+        n_launch = sum(launches_per_bench_step(p, s_start + k * MD_STEPS, tuning.get("form", 1))
+                       for k in range(K))
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / K, "higher_is_better": True,
@@ -607,7 +611,8 @@ def main() -> None:
             "config": workload_config(total),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "fused force + Langevin step (k_step)",
+                         "kernel": "force + Langevin step (k_step; + k_finish in the two-kernel "
+                                   "form)", "step_form": tuning.get("form"),
                          "bytes_per_launch": byts, "launch_us": t_kernel * 1e6,
                          "peak_source": peak_kind},
             "cpu_baseline": cpu,

@@ -80,6 +80,9 @@ typedef struct sop_params {
   int integrator;     /* 0: underdamped Langevin (sop.cu:421-462); 1: overdamped,
                          x += (h / zeta) f with f = F + noise (sop.cu:487-521,
                          a5 = h / zeta, param.cpp:110); velocities stay zero */
+  int step_split;     /* form of the step: 1 one kernel, 2 a force kernel and a
+                         finish kernel, 0 chosen by timing at commit (served
+                         contexts: 2).  Every form gives the same bits. */
 } sop_params;
 
 /* Fills *p with the reference's defaults and the factor-mode list cut-offs. */
@@ -229,6 +232,9 @@ int sop_memory(void* ctx, int mol, long long* ctx_bytes, long long* mol_bytes);
  * times in ms for those four candidates (0 when not tuned).  Forces are
  * bit-identical for every choice. */
 int sop_tuning(void* ctx, int* lanes, float* ms);
+/* The step's shape in use: lanes per bead, and its form (1 one kernel, 2 a
+ * force kernel and a finish kernel). */
+int sop_step_form(void* ctx, int* lanes, int* form);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that time or order
  * work around the engine. */

@@ -35,7 +35,7 @@ void launch_rebin(const DevSys& s, const NLScratch& w, cudaStream_t st);
 void launch_scan(const int* in, long long n, int* out, int* block_sums, cudaStream_t st);
 long long scan_block_sums_needed(long long n);
 // kernels_step.cu
-void launch_step(const DevSys& s, int G, int koff, bool step, cudaStream_t st);
+void launch_step(const DevSys& s, int G, bool split, int koff, bool step, cudaStream_t st);
 void launch_advance(const DevSys& s, int steps, cudaStream_t st);
 void launch_gather_current(const DevSys& s, float* out, cudaStream_t st);
 void launch_energy(const DevSys& s, int mol_start, int mol_n, int m, double* part, double* out,
@@ -177,11 +177,12 @@ struct SopCtx {
   long long bytes = 0;
   NLScratch w{};
   int G = 8;
+  bool split = false;         // step as force kernel + finish kernel
   double* e_part = nullptr;   // energy / observable partials
   double* e_out = nullptr;    // 8 doubles
   double* h_out = nullptr;    // pinned copy of e_out
   float4* stage = nullptr;    // gather buffer of sop_download_all
-  std::map<int, float> tuning;  // step-kernel time (ms) per lanes-per-bead candidate
+  std::map<int, float> tuning;  // step time (ms) per lanes-per-bead candidate (its faster form)
   Caps caps;
   MolConst* dmol = nullptr;
   RangeAlloc bead_alloc, bond_alloc, ang_alloc, nat_alloc;
@@ -267,31 +268,48 @@ int lanes_for(const SopCtx* ctx) {
   return 0;  // autotune
 }
 
-// Picks the lanes per bead G of the step kernel for this context by timing
-// the force-only kernel (idempotent: it recomputes the same forces and
-// look-ahead from the same state) for each G; results are bit-identical for
-// every G, so only the speed differs.
+// The step's form: 1 one kernel, 2 force kernel + finish kernel, 0 autotuned.
+int split_for(const SopCtx* ctx) {
+  const int f = ctx->P.step_split;
+  return (f == 1 || f == 2) ? f : 0;
+}
+
+// Picks the lanes per bead G and the form (one kernel or two) of the step for
+// this context by timing the force-only step (idempotent: it recomputes the
+// same forces and look-ahead from the same state) for each candidate not
+// fixed by the parameters; results are bit-identical for every G and form,
+// so only the speed differs.
 int autotune_lanes(SopCtx* ctx) {
+  const int fixed_g = lanes_for(ctx), fixed_f = split_for(ctx);
   const int cand[4] = {2, 4, 8, 16};
   cudaEvent_t a, b;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
   float best = 1e30f;
-  int bestg = 8;
+  int bestg = fixed_g ? fixed_g : 8;
+  bool bests = fixed_f == 2;
   for (int g : cand) {
-    launch_step(ctx->s, g, 0, false, ctx->stream);  // warm-up
-    CK(cudaEventRecord(a, ctx->stream));
-    for (int r = 0; r < 3; ++r) launch_step(ctx->s, g, 0, false, ctx->stream);
-    CK(cudaEventRecord(b, ctx->stream));
-    CK(cudaEventSynchronize(b));
-    float ms = 0.f;
-    CK(cudaEventElapsedTime(&ms, a, b));
-    ctx->tuning[g] = ms / 3.0f;
-    if (ms < best) { best = ms; bestg = g; }
+    if (fixed_g && g != fixed_g) continue;
+    float gbest = 1e30f;
+    for (int f = 1; f <= 2; ++f) {
+      if (fixed_f && f != fixed_f) continue;
+      const bool sp = f == 2;
+      launch_step(ctx->s, g, sp, 0, false, ctx->stream);  // warm-up
+      CK(cudaEventRecord(a, ctx->stream));
+      for (int r = 0; r < 3; ++r) launch_step(ctx->s, g, sp, 0, false, ctx->stream);
+      CK(cudaEventRecord(b, ctx->stream));
+      CK(cudaEventSynchronize(b));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, a, b));
+      gbest = std::min(gbest, ms / 3.0f);
+      if (ms < best) { best = ms; bestg = g; bests = sp; }
+    }
+    ctx->tuning[g] = gbest;
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   ctx->G = bestg;
+  ctx->split = bests;
   return SOP_OK;
 }
 
@@ -342,7 +360,7 @@ int nl_rebuild_checked(SopCtx* ctx, int koff) {
 }
 
 void force_eval_async(SopCtx* ctx) {
-  launch_step(ctx->s, ctx->G, 0, false, ctx->stream);
+  launch_step(ctx->s, ctx->G, ctx->split, 0, false, ctx->stream);
 }
 
 // Which rebuilds precede step n (1-based): bit 0 neighbour list, bit 1 pair list.
@@ -360,7 +378,7 @@ void enqueue_block(SopCtx* ctx, long long s0, int count) {
     int r = rebuilds_before(ctx->P, s0 + 1 + k);
     if (r & 1) launch_nl_rebuild(ctx->s, ctx->w, k, ctx->stream);
     if (r & 2) launch_pl_rebuild(ctx->s, k, ctx->stream);
-    launch_step(ctx->s, ctx->G, k, true, ctx->stream);
+    launch_step(ctx->s, ctx->G, ctx->split, k, true, ctx->stream);
   }
   launch_advance(ctx->s, count, ctx->stream);
 }
@@ -513,6 +531,7 @@ int alloc_pools(SopCtx* ctx, const Caps& c) {
   s.v = ctx->dalloc<float4>(nb);
   s.incr = ctx->dalloc<float4>(nb);
   s.f = ctx->dalloc<float4>(nb);
+  s.fsum = ctx->dalloc<float4>(nb);
   s.mol_of = ctx->dalloc<int>(nb);
   ctx->dmol = ctx->dalloc<MolConst>(nm);
   s.mol = ctx->dmol;
@@ -556,7 +575,7 @@ int alloc_pools(SopCtx* ctx, const Caps& c) {
   ctx->w.cells_total = ctx->dalloc<int>(1);
   ctx->e_part = ctx->dalloc<double>(6 * ((size_t)c.max_mol_beads / 256 + 2));
   ctx->e_out = ctx->dalloc<double>(8);
-  if (!s.x[0] || !s.x[1] || !s.p[0] || !s.p[1] || !s.v || !s.incr || !s.f || !s.mol_of ||
+  if (!s.x[0] || !s.x[1] || !s.p[0] || !s.p[1] || !s.v || !s.incr || !s.f || !s.fsum || !s.mol_of ||
       !s.mol || !s.mol_step || !s.mol_status || !s.sys_step || !s.bond_row || !s.ang_row ||
       !s.nat_row || !s.bond_j || !s.bond_r0 || !s.ang_j || !s.nat_j || !s.nat_par ||
       !s.nat_rc2 || !s.nl_att_cnt || !s.pl_att_cnt || !s.nl_att_e || !s.pl_att || !s.nl_cnt ||
@@ -567,6 +586,7 @@ int alloc_pools(SopCtx* ctx, const Caps& c) {
   if (!ctx->h_out) CK(cudaMallocHost(&ctx->h_out, 8 * sizeof(double)));
   cudaStream_t st = ctx->stream;
   CK(cudaMemsetAsync(s.mol_of, 0xff, sizeof(int) * nb, st));   // -1: free
+  CK(cudaMemsetAsync(s.fsum, 0, sizeof(float4) * nb, st));      // no step in flight
   CK(cudaMemsetAsync(ctx->dmol, 0, sizeof(MolConst) * nm, st));  // inactive
   CK(cudaMemsetAsync(s.mol_step, 0, sizeof(long long) * nm, st));
   CK(cudaMemsetAsync(s.mol_status, 0, sizeof(int) * nm, st));
@@ -777,8 +797,9 @@ int uninstall(SopCtx* ctx, int slot) {
 // Set-up after installing molecules at step 0: lists from x_0, f_0 and the
 // look-ahead (sop.cu:142-186), and the lanes-per-bead choice.
 int setup_step0(SopCtx* ctx) {
-  const int fixed_g = lanes_for(ctx);
+  const int fixed_g = lanes_for(ctx), fixed_f = split_for(ctx);
   ctx->G = fixed_g ? fixed_g : 8;
+  ctx->split = fixed_f == 2;
   // block offset -1: these rebuilds precede the force evaluation of the
   // current step itself (x_0 sits in both coordinate buffers)
   int rc = nl_rebuild_checked(ctx, -1);
@@ -786,7 +807,7 @@ int setup_step0(SopCtx* ctx) {
   launch_pl_rebuild(ctx->s, -1, ctx->stream);
   force_eval_async(ctx);
   CK(cudaGetLastError());
-  if (!fixed_g) {
+  if (!fixed_g || !fixed_f) {
     rc = autotune_lanes(ctx);
     if (rc) return rc;
   }
@@ -889,12 +910,14 @@ void sop_params_default(sop_params* p) {
   p->lanes_per_bead = 0;
   p->seed = 1234;       // setup_rng(1234, 0), sop.cu:138
   p->integrator = 0;    // underdamped (param.cpp:249-253 selects)
+  p->step_split = 0;    // autotuned
 }
 
 int sop_ctx_create(const sop_params* p, void** out) {
   if (!p || !out) return SOP_ERR_ARG;
   *out = nullptr;
   if (p->boxl <= 0 || p->h <= 0 || p->R0 <= 0 || p->graph_steps < 0 || p->integrator < 0 ||
+      p->step_split < 0 || p->step_split > 2 ||
       p->integrator > 1 || (p->integrator == 1 && p->zeta <= 0)) {
     g_lib_error = "invalid parameters";
     return SOP_ERR_ARG;
@@ -1355,8 +1378,12 @@ int sop_serve_create(const sop_params* p, long long budget_bytes, long long max_
   ctx->s.uniform_type = 1;
   ctx->mols.assign(c.mols, HostMol());
   ctx->slot_job.assign(c.mols, -1);
-  const int fixed_g = lanes_for(ctx);
+  // a served context fills up and empties as jobs come and go, so its step
+  // shape is fixed rather than timed once: 4 lanes per bead, two kernels
+  // (the faster form for a populated context) unless the parameters say
+  const int fixed_g = lanes_for(ctx), fixed_f = split_for(ctx);
   ctx->G = fixed_g ? fixed_g : 4;
+  ctx->split = fixed_f != 1;
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->committed = true;
   ctx->host_step = 0;
@@ -1528,7 +1555,7 @@ int sop_launch_stage(void* p, int stage, int koff) {
   SopCtx* ctx = C(p);
   if (!ctx->committed) return ctx->fail(SOP_ERR_ARG, "context not committed");
   switch (stage) {
-    case 0: launch_step(ctx->s, ctx->G, koff, true, ctx->stream); break;
+    case 0: launch_step(ctx->s, ctx->G, ctx->split, koff, true, ctx->stream); break;
     case 1: launch_pl_rebuild(ctx->s, koff, ctx->stream); break;
     case 2: launch_nl_rebuild(ctx->s, ctx->w, koff, ctx->stream); break;
     case 3: launch_advance(ctx->s, koff, ctx->stream); break;
@@ -1914,6 +1941,14 @@ int sop_tuning(void* p, int* lanes, float* ms) {
       ms[k] = it == ctx->tuning.end() ? 0.0f : it->second;
     }
   }
+  return SOP_OK;
+}
+
+int sop_step_form(void* p, int* lanes, int* form) {
+  if (!p) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (lanes) *lanes = ctx->G;
+  if (form) *form = ctx->split ? 2 : 1;
   return SOP_OK;
 }
 

@@ -85,13 +85,20 @@ __device__ __forceinline__ float small_coeff(const DevSys& s, int type, float dx
 
 // STEP = false: force evaluation only at step mol_step + koff (velocities kept),
 // followed by the look-ahead; used after set-up and state uploads.
-template <int G, bool STEP, bool UNI>
+template <bool STEP>
+__device__ __forceinline__ void finish_bead(const DevSys& s, int b, float4 fs, int koff);
+
+// SPLIT = false: one kernel -- the groups' sums go through shared memory to
+// one thread per bead, which completes the step (finish_bead).  SPLIT = true:
+// the sums go to s.fsum and k_finish completes the step in a second launch
+// (no block barrier, coalesced state access; faster for large contexts).
+// Both complete a bead with the same finish_bead, so the results are the
+// same bits.
+template <int G, bool STEP, bool UNI, bool SPLIT>
 __global__ void __launch_bounds__(256, StepBlocks<G>::value) k_step(DevSys s, int koff) {
   constexpr int BPB = 256 / G;          // beads per block
   pdl_wait();
   pdl_release();
-  __shared__ float4 fsum[BPB];          // conservative force sums; w = FENE range flag
-  __shared__ int bead[BPB];             // bead of each slot, -1: nothing to do
   const int slot = threadIdx.x / G;
   const int lane = threadIdx.x % G;
   const int k = blockIdx.x * BPB + slot; // position in cell order
@@ -237,23 +244,35 @@ __global__ void __launch_bounds__(256, StepBlocks<G>::value) k_step(DevSys s, in
     }
     fene_bad = __any_sync(gmask, fene_bad);
   }
-  const float fx = ax[0], fy = ay[0], fz = az[0];
+  const float4 sum = make_float4(ax[0], ay[0], az[0], fene_bad ? 2.0f : 1.0f);
+  if (SPLIT) {
+    // the group's sum, marked for k_finish (which completes the step)
+    if (i >= 0 && lane == 0) s.fsum[i] = sum;
+    return;
+  }
+  __shared__ float4 fsum[BPB];          // the slots' sums (w as in s.fsum)
+  __shared__ int bead[BPB];             // bead of each slot, -1: nothing to do
   if (lane == 0) {
-    fsum[slot] = make_float4(fx, fy, fz, fene_bad ? 1.0f : 0.0f);
+    fsum[slot] = sum;
     bead[slot] = i;
   }
   __syncthreads();
   if (threadIdx.x >= BPB) return;
-
-  // Per-bead epilogue, one thread per bead: noise, status, velocity and the
-  // look-ahead position update (sop.cu:421-462, energy.cu:588-604).
   const int b = bead[threadIdx.x];
   if (b < 0) return;
+  finish_bead<STEP>(s, b, fsum[threadIdx.x], koff);
+}
+
+// Completes bead b's step from its conservative force sum fs (w = 2: a bond
+// past R0): noise, status, velocity and the look-ahead position update
+// (sop.cu:421-462, energy.cu:588-604).  The step is the molecule's
+// mol_step + STEP + koff, as in k_step.  Every rounding is written out.
+template <bool STEP>
+__device__ __forceinline__ void finish_bead(const DevSys& s, int b, float4 fs, int koff) {
   const int m = s.mol_of[b];
   const MolConst mc = s.mol[m];
   const long long nb = s.mol_step[m] + (STEP ? 1 : 0) + koff;
   const int cur = (int)(nb & 1);
-  const float4 fs = fsum[threadIdx.x];
   float3 z;
   if (s.use_noise) {
     const float4 q = s.noise[b];
@@ -261,11 +280,11 @@ __global__ void __launch_bounds__(256, StepBlocks<G>::value) k_step(DevSys s, in
   } else {
     z = noise3((unsigned)(b - mc.start), nb, mc.traj, s.seed_lo, s.seed_hi);
   }
-  const float fxx = fs.x + mc.sigma_f * z.x;
-  const float fyy = fs.y + mc.sigma_f * z.y;
-  const float fzz = fs.z + mc.sigma_f * z.z;
+  const float fxx = __fmaf_rn(mc.sigma_f, z.x, fs.x);
+  const float fyy = __fmaf_rn(mc.sigma_f, z.y, fs.y);
+  const float fzz = __fmaf_rn(mc.sigma_f, z.z, fs.z);
   int st = 0;
-  if (fs.w != 0.0f) st |= SOP_MOL_FENE_RANGE;
+  if (fs.w == 2.0f) st |= SOP_MOL_FENE_RANGE;
   if (!(isfinite(fxx) && isfinite(fyy) && isfinite(fzz))) st |= SOP_MOL_NONFINITE;
   if (st) atomicOr(s.mol_status + m, st);
   s.f[b] = make_float4(fxx, fyy, fzz, 0.f);
@@ -273,19 +292,37 @@ __global__ void __launch_bounds__(256, StepBlocks<G>::value) k_step(DevSys s, in
   float4 inc = s.incr[b];
   // step 0 is the initial force evaluation (sop.cu:180-186): velocities stay
   if (STEP && nb > 0 && !mc.t_zero) {
-    vi = make_float4(mc.a3 * inc.x + mc.a4 * fxx, mc.a3 * inc.y + mc.a4 * fyy,
-                     mc.a3 * inc.z + mc.a4 * fzz, 0.f);
+    vi = make_float4(__fmaf_rn(mc.a3, inc.x, __fmul_rn(mc.a4, fxx)),
+                     __fmaf_rn(mc.a3, inc.y, __fmul_rn(mc.a4, fyy)),
+                     __fmaf_rn(mc.a3, inc.z, __fmul_rn(mc.a4, fzz)), 0.f);
     s.v[b] = vi;
   }
-  inc = make_float4(mc.a1 * vi.x + mc.a2 * fxx, mc.a1 * vi.y + mc.a2 * fyy,
-                    mc.a1 * vi.z + mc.a2 * fzz, 0.f);
+  inc = make_float4(__fmaf_rn(mc.a1, vi.x, __fmul_rn(mc.a2, fxx)),
+                    __fmaf_rn(mc.a1, vi.y, __fmul_rn(mc.a2, fyy)),
+                    __fmaf_rn(mc.a1, vi.z, __fmul_rn(mc.a2, fzz)), 0.f);
   s.incr[b] = inc;
   const float4 xo = s.x[cur][b];
-  s.x[cur ^ 1][b] = make_float4(xo.x + inc.x, xo.y + inc.y, xo.z + inc.z, xo.w);
+  s.x[cur ^ 1][b] = make_float4(__fadd_rn(xo.x, inc.x), __fadd_rn(xo.y, inc.y),
+                                __fadd_rn(xo.z, inc.z), xo.w);
   const float4 pi = s.p[cur][b];
   const float boxl = s.boxl;
-  s.p[cur ^ 1][b] = make_float4(min_image(pi.x + inc.x, boxl), min_image(pi.y + inc.y, boxl),
-                                min_image(pi.z + inc.z, boxl), 0.f);
+  s.p[cur ^ 1][b] = make_float4(min_image(__fadd_rn(pi.x, inc.x), boxl),
+                                min_image(__fadd_rn(pi.y, inc.y), boxl),
+                                min_image(__fadd_rn(pi.z, inc.z), boxl), 0.f);
+}
+
+// Second kernel of the split step: completes every bead k_step summed
+// (thread per bead, bead order, so every state access is coalesced).
+template <bool STEP>
+__global__ void __launch_bounds__(256) k_finish(DevSys s, int koff) {
+  pdl_wait();
+  pdl_release();
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= s.nbead) return;
+  const float4 fs = s.fsum[b];
+  if (fs.w == 0.0f) return;  // not summed this step
+  s.fsum[b].w = 0.0f;
+  finish_bead<STEP>(s, b, fs, koff);
 }
 
 // End of a block of `steps` steps: advance each running molecule's step
@@ -469,25 +506,35 @@ __global__ void k_gather_current(DevSys s, float* __restrict__ out) {
 // ----------------------------------------------------------- launchers
 static inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
-template <int G>
-static void launch_step_g(const DevSys& s, int koff, bool step, cudaStream_t st) {
+template <int G, bool SPLIT>
+static void launch_step_gs(const DevSys& s, int koff, bool step, cudaStream_t st) {
   const unsigned blocks = cdiv(s.nbead, 256 / G);
   if (s.uniform_type) {
-    if (step) launch_pdl(k_step<G, true, true>, blocks, 256, st, s, koff);
-    else launch_pdl(k_step<G, false, true>, blocks, 256, st, s, koff);
+    if (step) launch_pdl(k_step<G, true, true, SPLIT>, blocks, 256, st, s, koff);
+    else launch_pdl(k_step<G, false, true, SPLIT>, blocks, 256, st, s, koff);
   } else {
-    if (step) launch_pdl(k_step<G, true, false>, blocks, 256, st, s, koff);
-    else launch_pdl(k_step<G, false, false>, blocks, 256, st, s, koff);
+    if (step) launch_pdl(k_step<G, true, false, SPLIT>, blocks, 256, st, s, koff);
+    else launch_pdl(k_step<G, false, false, SPLIT>, blocks, 256, st, s, koff);
+  }
+  if (SPLIT) {
+    if (step) launch_pdl(k_finish<true>, cdiv(s.nbead, 256), 256, st, s, koff);
+    else launch_pdl(k_finish<false>, cdiv(s.nbead, 256), 256, st, s, koff);
   }
 }
 
-// Lanes per bead G in {2, 4, 8, 16}.
-void launch_step(const DevSys& s, int G, int koff, bool step, cudaStream_t st) {
+template <int G>
+static void launch_step_g(const DevSys& s, bool split, int koff, bool step, cudaStream_t st) {
+  if (split) launch_step_gs<G, true>(s, koff, step, st);
+  else launch_step_gs<G, false>(s, koff, step, st);
+}
+
+// Lanes per bead G in {2, 4, 8, 16}; split: force kernel + finish kernel.
+void launch_step(const DevSys& s, int G, bool split, int koff, bool step, cudaStream_t st) {
   switch (G) {
-    case 2: launch_step_g<2>(s, koff, step, st); break;
-    case 4: launch_step_g<4>(s, koff, step, st); break;
-    case 16: launch_step_g<16>(s, koff, step, st); break;
-    default: launch_step_g<8>(s, koff, step, st); break;
+    case 2: launch_step_g<2>(s, split, koff, step, st); break;
+    case 4: launch_step_g<4>(s, split, koff, step, st); break;
+    case 16: launch_step_g<16>(s, split, koff, step, st); break;
+    default: launch_step_g<8>(s, split, koff, step, st); break;
   }
 }
 

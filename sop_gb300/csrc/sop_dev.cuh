@@ -74,6 +74,8 @@ struct DevSys {
   float4* v;
   float4* incr;
   float4* f;
+  float4* fsum;                 // conservative force of the step being taken; w: 0 idle,
+                                // 1 summed, 2 summed with a bond past R0
   int* mol_of;
   const MolConst* mol;
   long long* mol_step;          // last completed step of each molecule (< 0: starts later)

@@ -51,7 +51,7 @@ class Params(ctypes.Structure):
                 ("nnlup", ctypes.c_int), ("nplup", ctypes.c_int), ("rep6", ctypes.c_int),
                 ("device", ctypes.c_int), ("graph_steps", ctypes.c_int),
                 ("lanes_per_bead", ctypes.c_int), ("seed", ctypes.c_ulonglong),
-                ("integrator", ctypes.c_int)]
+                ("integrator", ctypes.c_int), ("step_split", ctypes.c_int)]
 
 
 class MoleculeDesc(ctypes.Structure):
@@ -138,6 +138,7 @@ def lib() -> ctypes.CDLL:
             "sop_serve_result": (I, [V, I, V, V, V, ctypes.POINTER(I), PLL,
                                      ctypes.POINTER(ctypes.c_double)]),
             "sop_serve_stats": (I, [V, V]),
+            "sop_step_form": (I, [V, ctypes.POINTER(I), ctypes.POINTER(I)]),
             "sop_checkpoint": (I, [V, I, V, LL, PLL]),
             "sop_restore": (I, [V, I, V, LL]),
             "sop_serve_checkpoint": (I, [V, I, V, LL, PLL]),
@@ -342,7 +343,9 @@ class Engine:
         g = ctypes.c_int()
         ms = np.zeros(4, np.float32)
         self._check(lib().sop_tuning(self.h, ctypes.byref(g), _p(ms)), self.h)
-        return {"lanes_per_bead": g.value,
+        form = ctypes.c_int()
+        self._check(lib().sop_step_form(self.h, None, ctypes.byref(form)), self.h)
+        return {"lanes_per_bead": g.value, "form": form.value,
                 "ms": {str(k): float(v) for k, v in zip((2, 4, 8, 16), ms)}}
 
     def stream(self) -> int:

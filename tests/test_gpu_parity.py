@@ -268,16 +268,20 @@ def test_batched_equals_alone():
 
 
 def test_lanes_per_bead_bit_identical():
-    """The force summation order does not depend on the lanes per bead, so
-    trajectories are bit-identical for every G (and G can be tuned freely)."""
+    """The force summation order does not depend on the lanes per bead, and
+    both forms of the step (one kernel; force + finish kernels) complete a
+    bead with the same code, so trajectories are bit-identical for every G
+    and form (both can be tuned freely)."""
     mol = mol_of(4000, 1)
     outs = []
     for g in (2, 4, 8, 16):
-        p = engine.baseline_params(lanes_per_bead=g)
-        with engine.plain(mol, mol.xyz, p, T=0.6, traj=2) as e:
-            assert e.tuning()["lanes_per_bead"] == g
-            e.step(30)
-            outs.append(e.download())
+        for form in (1, 2):
+            p = engine.baseline_params(lanes_per_bead=g, step_split=form)
+            with engine.plain(mol, mol.xyz, p, T=0.6, traj=2) as e:
+                t = e.tuning()
+                assert t["lanes_per_bead"] == g and t["form"] == form
+                e.step(30)
+                outs.append(e.download())
     for o in outs[1:]:
         for k in ("unc_pos", "vel", "force"):
             np.testing.assert_array_equal(o[k], outs[0][k])
@@ -287,7 +291,7 @@ def test_autotune_picks_a_candidate():
     mol = mol_of(4000, 1)
     with engine.plain(mol, mol.xyz, engine.baseline_params()) as e:
         t = e.tuning()
-    assert t["lanes_per_bead"] in (2, 4, 8, 16)
+    assert t["lanes_per_bead"] in (2, 4, 8, 16) and t["form"] in (1, 2)
     assert all(v > 0 for v in t["ms"].values())
 
 
