@@ -454,6 +454,8 @@ def main() -> None:
     ap.add_argument("--no-served", action="store_true", help="skip the served request stream")
     ap.add_argument("--lanes", type=int, default=0,
                     help="lanes per bead of the step kernel (2, 4, 8, 16); 0: autotuned")
+    ap.add_argument("--form", type=int, default=0,
+                    help="form of the step: 1 one kernel, 2 force + finish kernels; 0: autotuned")
     ap.add_argument("--workload", default="ensemble", choices=["ensemble", *PLAIN],
                     help="ensemble: the batched ensemble (with the served stream beside it); "
                          "plain128 / plain4000 / plain50k: the plain path on one structure")
@@ -490,7 +492,8 @@ def main() -> None:
 
     mols, ts = ensemble(rank)
     total = sum(m.n for m in mols)
-    p = engine.baseline_params(device=local, graph_steps=MD_STEPS, lanes_per_bead=args.lanes)
+    p = engine.baseline_params(device=local, graph_steps=MD_STEPS, lanes_per_bead=args.lanes,
+                               step_split=args.form)
     e = engine.Engine(p)
     for k, (m, t) in enumerate(zip(mols, ts)):
         e.add(m, m.xyz, T=float(t), traj=rank * N_TRAJ + k)
