@@ -104,6 +104,12 @@ struct RangeAlloc {
       }
     }
   }
+  // one past the last allocated position (0 when nothing is allocated)
+  long long high_water() const {
+    if (free_.empty()) return cap;
+    auto last = std::prev(free_.end());
+    return last->first + last->second == cap ? last->first : cap;
+  }
   long long largest() const {
     long long m = 0;
     for (auto& kv : free_) m = std::max(m, kv.second);
@@ -523,6 +529,7 @@ int alloc_pools(SopCtx* ctx, const Caps& c) {
   ctx->caps = c;
   const size_t nb = (size_t)c.beads, nm = (size_t)c.mols;
   s.nbead = (int)c.beads;
+  s.nlive = s.nbead;
   s.nmol = (int)c.mols;
   for (int b = 0; b < 2; ++b) {
     s.x[b] = ctx->dalloc<float4>(nb);
@@ -1255,6 +1262,20 @@ bool ckpt_head(const void* buf, long long len, CkptHeader* h) {
          len == ckpt_bytes(h->n, h->cnt);
 }
 
+// The per-step kernels of a served context cover the bead slots up to the
+// highest one in use, rounded up to a sixteenth of the pool: the step graphs
+// hold that bound, so they are re-captured only when it crosses a sixteenth.
+static void update_live(SopCtx* ctx) {
+  const long long cap = ctx->caps.beads;
+  const long long g = std::max<long long>(1, (cap + 15) / 16);
+  const long long hw = ctx->bead_alloc.high_water();
+  const long long live = std::min(cap, std::max(g, (hw + g - 1) / g * g));
+  if (live != ctx->s.nlive) {
+    ctx->s.nlive = (int)live;
+    ctx->drop_graphs();  // kernel arguments changed
+  }
+}
+
 static int serve_round(SopCtx* ctx) {
   int rc = sync_checked(ctx);
   if (rc) return rc;
@@ -1309,6 +1330,7 @@ static int serve_round(SopCtx* ctx) {
     jb.mol = HostMol();
     it = ctx->queue.erase(it);
   }
+  update_live(ctx);
   if (rebin) {
     launch_rebin(ctx->s, ctx->w, ctx->stream);
     CK(cudaGetLastError());

@@ -132,7 +132,7 @@ __device__ __forceinline__ const float4* xbuf(const DevSys& s, int m, int koff) 
 
 __global__ void k_bbox(DevSys s, int koff) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  int m = (i < s.nbead) ? s.mol_of[i] : -1;
+  int m = (i < s.nlive) ? s.mol_of[i] : -1;
   bool ok = mol_listed(s, m, koff);
   unsigned act = __ballot_sync(0xffffffffu, ok);
   if (!ok) return;
@@ -247,7 +247,7 @@ __device__ __forceinline__ int cell_coord(float v, float lo, float cs, int dim) 
 // neighbour-list filter of its native row (sop.cu:704-759 semantics).
 __global__ void k_assign(DevSys s, int koff, int att) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= s.nbead) return;
+  if (i >= s.nlive) return;
   int m = s.mol_of[i];
   if (!mol_listed(s, m, koff)) {  // not binned; its lists stay as they are
     s.bead_cell[i] = -1;
@@ -289,7 +289,7 @@ __global__ void k_assign(DevSys s, int koff, int att) {
 
 __global__ void k_scatter(DevSys s) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= s.nbead) return;
+  if (i >= s.nlive) return;
   int c = s.bead_cell[i];
   if (c < 0) return;
   s.sorted[s.cell_start[c] + s.bead_slot[i]] = i;
@@ -450,11 +450,11 @@ __global__ void __launch_bounds__(256) k_pl(DevSys s, int koff) {
   const int wl = threadIdx.x & 31;
   const int lane = wl & (kPlLanes - 1);
   const unsigned gmask = ((1u << kPlLanes) - 1u) << (wl & ~(kPlLanes - 1));
-  // beads in cell order: the groups of a block gather from the same region
-  const int kk = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) / kPlLanes);
-  if (kk >= s.cell_start[s.cell_cap]) return;
+  // beads in chain order: the groups of a block gather from the same region
+  // of a molecule, and the per-bead loads are coalesced
+  const int i = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) / kPlLanes);
+  if (i >= s.nlive) return;
   if (*s.flags & FLAG_NL_OVERFLOW) return;
-  const int i = s.sorted[kk];
   const int m = s.mol_of[i];
   if (!mol_listed(s, m, koff)) return;  // finished or stopped: keeps the lists of its last step
   const float4* X = xbuf(s, m, koff);
@@ -471,10 +471,14 @@ __global__ void __launch_bounds__(256) k_pl(DevSys s, int koff) {
   const int2 row = s.nat_row[i];
   const int acnt = s.nl_att_cnt[i];
   int k = 0;
+  // each round works on entries loaded the round before (rows are read ahead)
+  int4 jn = make_int4(i, i, i, i);
+  if (4 * lane < cnt) jn = row4[lane];
   for (int e0 = 0; e0 < cnt; e0 += 4 * kPlLanes) {
     const int e = e0 + 4 * lane;
-    int4 jv = make_int4(i, i, i, i);
-    if (e < cnt) jv = row4[(e0 >> 2) + lane];
+    const int4 jv = jn;
+    jn = make_int4(i, i, i, i);
+    if (e + 4 * kPlLanes < cnt) jn = row4[(e0 >> 2) + kPlLanes + lane];
     const int jq[4] = {jv.x, e + 1 < cnt ? jv.y : i, e + 2 < cnt ? jv.z : i, e + 3 < cnt ? jv.w : i};
     unsigned pb = 0;
     int c = 0;
@@ -551,13 +555,13 @@ struct NLScratch {
 static void launch_binning(const DevSys& s, const NLScratch& w, int koff, int att, cudaStream_t st) {
   const int T = 256;
   k_bbox_reset<<<cdiv(s.nmol, T), T, 0, st>>>(s);
-  k_bbox<<<cdiv(s.nbead, T), T, 0, st>>>(s, koff);
+  k_bbox<<<cdiv(s.nlive, T), T, 0, st>>>(s, koff);
   k_grid<<<cdiv(s.nmol, T), T, 0, st>>>(s, w.ncell, koff);
   k_grid_base<<<1, 1024, 0, st>>>(s, w.ncell, w.cells_total);
   cudaMemsetAsync(s.cell_cnt, 0, sizeof(int) * (size_t)s.cell_cap, st);
-  k_assign<<<cdiv(s.nbead, T), T, 0, st>>>(s, koff, att);
+  k_assign<<<cdiv(s.nlive, T), T, 0, st>>>(s, koff, att);
   launch_scan(s.cell_cnt, s.cell_cap, s.cell_start, w.block_sums, st);
-  k_scatter<<<cdiv(s.nbead, T), T, 0, st>>>(s);
+  k_scatter<<<cdiv(s.nlive, T), T, 0, st>>>(s);
   k_cellsort<<<cdiv(s.cell_cap, T), T, 0, st>>>(s, koff, w.cells_total);
 }
 
@@ -566,9 +570,9 @@ void launch_nl_rebuild(const DevSys& s, const NLScratch& w, int koff, cudaStream
   const int T = 256;
   launch_binning(s, w, koff, 1, st);
   if (s.uniform_type)
-    k_nl<true><<<cdiv((long long)s.nbead * kNlLanes, T), T, 0, st>>>(s);
+    k_nl<true><<<cdiv((long long)s.nlive * kNlLanes, T), T, 0, st>>>(s);
   else
-    k_nl<false><<<cdiv((long long)s.nbead * kNlLanes, T), T, 0, st>>>(s);
+    k_nl<false><<<cdiv((long long)s.nlive * kNlLanes, T), T, 0, st>>>(s);
 }
 
 // The cell order alone, every list untouched: puts molecules that arrive
@@ -581,9 +585,9 @@ void launch_rebin(const DevSys& s, const NLScratch& w, cudaStream_t st) {
 void launch_pl_rebuild(const DevSys& s, int koff, cudaStream_t st) {
   const int T = 256;
   if (s.uniform_type)
-    launch_pdl(k_pl<true>, cdiv((long long)s.nbead * kPlLanes, T), T, st, s, koff);
+    launch_pdl(k_pl<true>, cdiv((long long)s.nlive * kPlLanes, T), T, st, s, koff);
   else
-    launch_pdl(k_pl<false>, cdiv((long long)s.nbead * kPlLanes, T), T, st, s, koff);
+    launch_pdl(k_pl<false>, cdiv((long long)s.nlive * kPlLanes, T), T, st, s, koff);
 }
 
 }  // namespace sop

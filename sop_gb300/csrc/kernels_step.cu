@@ -5,8 +5,9 @@
 // The reference runs per step underdamped_iteration_kernel (sop.cu:421-447),
 // clear_forces + rand_kernel + four force kernels with float atomics
 // (energy.cu:54-167, 228-584) and update_velocities_kernel (sop.cu:450-462).
-// Here a group of G lanes owns a bead (beads taken in cell order, so
-// neighbouring groups gather from the same region): it sums the bead's force
+// Here a group of G lanes owns a bead (beads in chain order: neighbouring
+// groups gather from the same region of a molecule, and the per-bead loads
+// are coalesced): it sums the bead's force
 // over its own full rows (every pair is stored for both beads) in an order
 // that does not depend on G, then one thread per bead adds the noise and
 // updates velocity and coordinates.  No atomics.
@@ -24,10 +25,12 @@ namespace sop {
 
 constexpr int kV = 16;  // virtual lanes of the fixed force-summation order
 
+constexpr int kStepThreads = 128;  // small blocks: a finished block frees its SM slot sooner
+
 // Blocks per SM each lane-group width is compiled for (a register cap).
 template <int G>
 struct StepBlocks {
-  static constexpr int value = G == 4 ? 5 : (G == 8 ? 6 : (G == 16 ? 4 : 1));
+  static constexpr int value = G == 4 ? 10 : (G == 8 ? 12 : (G == 16 ? 8 : 2));
 };
 
 // Every rounding of the per-entry arithmetic and of the accumulation is
@@ -95,19 +98,28 @@ __device__ __forceinline__ void finish_bead(const DevSys& s, int b, float4 fs, i
 // Both complete a bead with the same finish_bead, so the results are the
 // same bits.
 template <int G, bool STEP, bool UNI, bool SPLIT>
-__global__ void __launch_bounds__(256, StepBlocks<G>::value) k_step(DevSys s, int koff) {
-  constexpr int BPB = 256 / G;          // beads per block
+__global__ void __launch_bounds__(kStepThreads, StepBlocks<G>::value) k_step(DevSys s, int koff) {
+  constexpr int BPB = kStepThreads / G;  // beads per block
   pdl_wait();
   pdl_release();
   const int slot = threadIdx.x / G;
   const int lane = threadIdx.x % G;
-  const int k = blockIdx.x * BPB + slot; // position in cell order
-  const int nbinned = s.cell_start[s.cell_cap];
   int i = -1;
   long long n = 0;
-  const int b1 = (k < nbinned && !(*s.flags & FLAG_NL_OVERFLOW)) ? s.sorted[k] : -1;
-  // the cell order is from the last rebuild: a slot freed since then has no molecule
-  const int m1 = b1 >= 0 ? s.mol_of[b1] : -1;
+  const int b1 = blockIdx.x * BPB + slot;
+  const bool live = b1 < s.nlive && !(*s.flags & FLAG_NL_OVERFLOW);
+  const int m1 = live ? s.mol_of[b1] : -1;  // -1: a free slot
+  // Row descriptors, loaded beside the molecule's state rather than after
+  // its test: they do not depend on it.
+  int2 br = make_int2(0, 0), ar = make_int2(0, 0);
+  int abase = 0, acnt = 0, rcnt = 0;
+  if (live) {
+    br = s.bond_row[b1];
+    ar = s.ang_row[b1];
+    abase = s.nat_row[b1].x;
+    acnt = s.pl_att_cnt[b1];
+    rcnt = s.pl_cnt[b1];
+  }
   if (m1 >= 0) {
     const MolConst& mc = s.mol[m1];
     n = s.mol_step[m1] + (STEP ? 1 : 0) + koff;
@@ -137,13 +149,7 @@ __global__ void __launch_bounds__(256, StepBlocks<G>::value) k_step(DevSys s, in
     // with a cut-off of margin): the minimum image is then the identity and
     // its test is skipped
     const bool wrap = s.grid[m1].wrap != 0;
-    // Row descriptors first, as independent loads.
-    const int2 br = s.bond_row[i];
-    const int2 ar = s.ang_row[i];
-    const int abase = s.nat_row[i].x;
-    const int acnt = s.pl_att_cnt[i];
     const long long rbase = (long long)i * s.nl_stride;
-    const int rcnt = s.pl_cnt[i];
 
     // Bonded, angle and native terms share one index space [bonds | angles |
     // natives]; a bead has a handful of them, usually one pass.
@@ -318,7 +324,7 @@ __global__ void __launch_bounds__(256) k_finish(DevSys s, int koff) {
   pdl_wait();
   pdl_release();
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= s.nbead) return;
+  if (b >= s.nlive) return;
   const float4 fs = s.fsum[b];
   if (fs.w == 0.0f) return;  // not summed this step
   s.fsum[b].w = 0.0f;
@@ -508,17 +514,18 @@ static inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b
 
 template <int G, bool SPLIT>
 static void launch_step_gs(const DevSys& s, int koff, bool step, cudaStream_t st) {
-  const unsigned blocks = cdiv(s.nbead, 256 / G);
+  const unsigned blocks = cdiv(s.nlive, kStepThreads / G);
+  const int T = kStepThreads;
   if (s.uniform_type) {
-    if (step) launch_pdl(k_step<G, true, true, SPLIT>, blocks, 256, st, s, koff);
-    else launch_pdl(k_step<G, false, true, SPLIT>, blocks, 256, st, s, koff);
+    if (step) launch_pdl(k_step<G, true, true, SPLIT>, blocks, T, st, s, koff);
+    else launch_pdl(k_step<G, false, true, SPLIT>, blocks, T, st, s, koff);
   } else {
-    if (step) launch_pdl(k_step<G, true, false, SPLIT>, blocks, 256, st, s, koff);
-    else launch_pdl(k_step<G, false, false, SPLIT>, blocks, 256, st, s, koff);
+    if (step) launch_pdl(k_step<G, true, false, SPLIT>, blocks, T, st, s, koff);
+    else launch_pdl(k_step<G, false, false, SPLIT>, blocks, T, st, s, koff);
   }
   if (SPLIT) {
-    if (step) launch_pdl(k_finish<true>, cdiv(s.nbead, 256), 256, st, s, koff);
-    else launch_pdl(k_finish<false>, cdiv(s.nbead, 256), 256, st, s, koff);
+    if (step) launch_pdl(k_finish<true>, cdiv(s.nlive, 256), 256, st, s, koff);
+    else launch_pdl(k_finish<false>, cdiv(s.nlive, 256), 256, st, s, koff);
   }
 }
 

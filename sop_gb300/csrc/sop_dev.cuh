@@ -55,6 +55,7 @@ struct MolGrid {
 
 struct DevSys {
   int nbead, nmol;
+  int nlive;                    // bead slots the per-step kernels cover; every slot past it is free
   float boxl;
   float eps_rep;
   int rep6;
