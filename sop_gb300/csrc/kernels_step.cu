@@ -88,8 +88,13 @@ __device__ __forceinline__ float small_coeff(const DevSys& s, int type, float dx
 
 // STEP = false: force evaluation only at step mol_step + koff (velocities kept),
 // followed by the look-ahead; used after set-up and state uploads.
+// Marker bits in the w of a bead's force sum (0: not summed this step).
+constexpr int kSummed = 1;
+constexpr int kFeneBad = 2;   // a bond at or past R0
+constexpr int kOddStep = 4;   // the step is odd: coordinates in buffer 1
+
 template <bool STEP>
-__device__ __forceinline__ void finish_bead(const DevSys& s, int b, float4 fs, int koff);
+__device__ __forceinline__ void finish_bead(const DevSys& s, int b, int m, float4 fs, int koff);
 
 // SPLIT = false: one kernel -- the groups' sums go through shared memory to
 // one thread per bead, which completes the step (finish_bead).  SPLIT = true:
@@ -250,7 +255,11 @@ __global__ void __launch_bounds__(kStepThreads, StepBlocks<G>::value) k_step(Dev
     }
     fene_bad = __any_sync(gmask, fene_bad);
   }
-  const float4 sum = make_float4(ax[0], ay[0], az[0], fene_bad ? 2.0f : 1.0f);
+  // w: the marker bits of finish_bead (summed, a bond past R0, the parity of
+  // the step, which selects the coordinate buffers)
+  const float4 sum = make_float4(ax[0], ay[0], az[0],
+                                 __int_as_float(kSummed | (fene_bad ? kFeneBad : 0) |
+                                                ((int)(n & 1) ? kOddStep : 0)));
   if (SPLIT) {
     // the group's sum, marked for k_finish (which completes the step)
     if (i >= 0 && lane == 0) s.fsum[i] = sum;
@@ -266,19 +275,25 @@ __global__ void __launch_bounds__(kStepThreads, StepBlocks<G>::value) k_step(Dev
   if (threadIdx.x >= BPB) return;
   const int b = bead[threadIdx.x];
   if (b < 0) return;
-  finish_bead<STEP>(s, b, fsum[threadIdx.x], koff);
+  finish_bead<STEP>(s, b, s.mol_of[b], fsum[threadIdx.x], koff);
 }
 
-// Completes bead b's step from its conservative force sum fs (w = 2: a bond
-// past R0): noise, status, velocity and the look-ahead position update
-// (sop.cu:421-462, energy.cu:588-604).  The step is the molecule's
-// mol_step + STEP + koff, as in k_step.  Every rounding is written out.
+// Completes bead b (of molecule m) from its conservative force sum fs, whose
+// w holds the marker bits k_step set: noise, status, velocity and the
+// look-ahead position update (sop.cu:421-462, energy.cu:588-604).  The step
+// is the molecule's mol_step + STEP + koff, as in k_step.  Every load is
+// issued before any store (they are independent), and every rounding is
+// written out.
 template <bool STEP>
-__device__ __forceinline__ void finish_bead(const DevSys& s, int b, float4 fs, int koff) {
-  const int m = s.mol_of[b];
+__device__ __forceinline__ void finish_bead(const DevSys& s, int b, int m, float4 fs, int koff) {
+  const int w = __float_as_int(fs.w);
+  const int cur = (w & kOddStep) ? 1 : 0;
   const MolConst mc = s.mol[m];
   const long long nb = s.mol_step[m] + (STEP ? 1 : 0) + koff;
-  const int cur = (int)(nb & 1);
+  float4 vi = s.v[b];
+  float4 inc = s.incr[b];
+  const float4 xo = s.x[cur][b];
+  const float4 pi = s.p[cur][b];
   float3 z;
   if (s.use_noise) {
     const float4 q = s.noise[b];
@@ -290,12 +305,10 @@ __device__ __forceinline__ void finish_bead(const DevSys& s, int b, float4 fs, i
   const float fyy = __fmaf_rn(mc.sigma_f, z.y, fs.y);
   const float fzz = __fmaf_rn(mc.sigma_f, z.z, fs.z);
   int st = 0;
-  if (fs.w == 2.0f) st |= SOP_MOL_FENE_RANGE;
+  if (w & kFeneBad) st |= SOP_MOL_FENE_RANGE;
   if (!(isfinite(fxx) && isfinite(fyy) && isfinite(fzz))) st |= SOP_MOL_NONFINITE;
   if (st) atomicOr(s.mol_status + m, st);
   s.f[b] = make_float4(fxx, fyy, fzz, 0.f);
-  float4 vi = s.v[b];
-  float4 inc = s.incr[b];
   // step 0 is the initial force evaluation (sop.cu:180-186): velocities stay
   if (STEP && nb > 0 && !mc.t_zero) {
     vi = make_float4(__fmaf_rn(mc.a3, inc.x, __fmul_rn(mc.a4, fxx)),
@@ -307,10 +320,8 @@ __device__ __forceinline__ void finish_bead(const DevSys& s, int b, float4 fs, i
                     __fmaf_rn(mc.a1, vi.y, __fmul_rn(mc.a2, fyy)),
                     __fmaf_rn(mc.a1, vi.z, __fmul_rn(mc.a2, fzz)), 0.f);
   s.incr[b] = inc;
-  const float4 xo = s.x[cur][b];
   s.x[cur ^ 1][b] = make_float4(__fadd_rn(xo.x, inc.x), __fadd_rn(xo.y, inc.y),
                                 __fadd_rn(xo.z, inc.z), xo.w);
-  const float4 pi = s.p[cur][b];
   const float boxl = s.boxl;
   s.p[cur ^ 1][b] = make_float4(min_image(__fadd_rn(pi.x, inc.x), boxl),
                                 min_image(__fadd_rn(pi.y, inc.y), boxl),
@@ -326,9 +337,10 @@ __global__ void __launch_bounds__(256) k_finish(DevSys s, int koff) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= s.nlive) return;
   const float4 fs = s.fsum[b];
-  if (fs.w == 0.0f) return;  // not summed this step
+  const int m = s.mol_of[b];
+  if (__float_as_int(fs.w) == 0) return;  // not summed this step
   s.fsum[b].w = 0.0f;
-  finish_bead<STEP>(s, b, fs, koff);
+  finish_bead<STEP>(s, b, m, fs, koff);
 }
 
 // End of a block of `steps` steps: advance each running molecule's step

@@ -76,7 +76,7 @@ struct DevSys {
   float4* incr;
   float4* f;
   float4* fsum;                 // conservative force of the step being taken; w: 0 idle,
-                                // 1 summed, 2 summed with a bond past R0
+                                // else marker bits (summed, a bond past R0, odd step)
   int* mol_of;
   const MolConst* mol;
   long long* mol_step;          // last completed step of each molecule (< 0: starts later)
