@@ -331,7 +331,7 @@ __device__ __forceinline__ void finish_bead(const DevSys& s, int b, int m, float
 // Second kernel of the split step: completes every bead k_step summed
 // (thread per bead, bead order, so every state access is coalesced).
 template <bool STEP>
-__global__ void __launch_bounds__(256) k_finish(DevSys s, int koff) {
+__global__ void __launch_bounds__(256, 6) k_finish(DevSys s, int koff) {
   pdl_wait();
   pdl_release();
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
