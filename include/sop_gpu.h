@@ -210,6 +210,22 @@ int sop_list_sizes(void* ctx, long long* out);
 int sop_download_all(void* ctx, float* unc_pos);
 
 /*
+ * sop_download_all without the waits: queues a gather of the coordinates
+ * the queued work will have reached, and their copy into unc_pos on a copy
+ * stream of the context, so that the copy overlaps the steps queued after
+ * it.  Returns at once (when unc_pos is page-locked host memory) with a
+ * ticket.  sop_download_wait(ticket) waits for that copy; it returns
+ * SOP_ERR_CAPACITY when the neighbour lists had overflowed before the
+ * gather (the coordinates are then those of the frozen molecules: sop_sync
+ * re-runs the frozen steps, and a new download gives the right ones).
+ * unc_pos must stay valid until the wait.  Two downloads may be in flight;
+ * a third waits on the device for the first one's copy.  The reference
+ * reads back with blocking copies (sop.cu:252-263).
+ */
+int sop_download_all_async(void* ctx, float* unc_pos, long long* ticket);
+int sop_download_wait(void* ctx, long long ticket);
+
+/*
  * Energy terms of molecule `mol` on its current pair lists (energy_eval and
  * the host energies of energy.cu:69-78, 194-225, 278-307, 369-442), per-term
  * FP32 evaluation with an FP64 final sum.  terms: e_bnd, e_ang_ss,

@@ -37,7 +37,7 @@ long long scan_block_sums_needed(long long n);
 // kernels_step.cu
 void launch_step(const DevSys& s, int G, bool split, int koff, bool step, cudaStream_t st);
 void launch_advance(const DevSys& s, int steps, cudaStream_t st);
-void launch_gather_current(const DevSys& s, float* out, cudaStream_t st);
+void launch_gather_current(const DevSys& s, float* out, int* flag_out, cudaStream_t st);
 void launch_energy(const DevSys& s, int mol_start, int mol_n, int m, double* part, double* out,
                    double k_bnd_R0sq_half, cudaStream_t st);
 void launch_observables(const DevSys& s, int mol_start, int mol_n, int m, int nnat,
@@ -188,6 +188,15 @@ struct SopCtx {
   double* e_out = nullptr;    // 8 doubles
   double* h_out = nullptr;    // pinned copy of e_out
   float4* stage = nullptr;    // gather buffer of sop_download_all
+  // sop_download_all_async: two gather buffers (packed xyz, then the
+  // overflow flag the gather saw), a copy stream, and per buffer the events
+  // of its gather and of its copy to the host
+  cudaStream_t copy_stream = nullptr;
+  float4* astage[2] = {nullptr, nullptr};
+  cudaEvent_t gathered[2] = {nullptr, nullptr};
+  cudaEvent_t copied[2] = {nullptr, nullptr};
+  int* h_flag = nullptr;      // pinned: the flag of each buffer's last copy
+  long long next_ticket = 0;
   std::map<int, float> tuning;  // step time (ms) per lanes-per-bead candidate (its faster form)
   Caps caps;
   MolConst* dmol = nullptr;
@@ -248,6 +257,16 @@ struct SopCtx {
     graphs.clear();
   }
   void release() {
+    if (copy_stream) cudaStreamSynchronize(copy_stream);  // copies into caller memory
+    for (int k = 0; k < 2; ++k) {
+      if (gathered[k]) cudaEventDestroy(gathered[k]);
+      if (copied[k]) cudaEventDestroy(copied[k]);
+      gathered[k] = copied[k] = nullptr;
+    }
+    if (copy_stream) cudaStreamDestroy(copy_stream);
+    copy_stream = nullptr;
+    if (h_flag) cudaFreeHost(h_flag);
+    h_flag = nullptr;
     drop_graphs();
     for (void* p : allocs) cudaFree(p);
     allocs.clear();
@@ -1569,7 +1588,10 @@ int sop_sync(void* p) {
   if (!p) return SOP_ERR_ARG;
   SopCtx* ctx = C(p);
   if (!ctx->committed) return ctx->fail(SOP_ERR_ARG, "context not committed");
-  return sync_checked(ctx);
+  int rc = sync_checked(ctx);
+  if (rc) return rc;
+  if (ctx->copy_stream) CK(cudaStreamSynchronize(ctx->copy_stream));
+  return SOP_OK;
 }
 
 int sop_launch_stage(void* p, int stage, int koff) {
@@ -1783,11 +1805,62 @@ int sop_download_all(void* p, float* unc_pos) {
   }
   // the staging buffer (nbead float4) holds the packed 3 * nbead floats
   float* packed = reinterpret_cast<float*>(ctx->stage);
-  launch_gather_current(ctx->s, packed, ctx->stream);
+  launch_gather_current(ctx->s, packed, nullptr, ctx->stream);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(unc_pos, packed, sizeof(float) * 3 * (size_t)ctx->s.nbead,
                      cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  return SOP_OK;
+}
+
+int sop_download_all_async(void* p, float* unc_pos, long long* ticket) {
+  if (!p || !unc_pos || !ticket) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (!ctx->committed) return ctx->fail(SOP_ERR_ARG, "context not committed");
+  if (!ctx->copy_stream) {
+    CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+      CK(cudaEventCreateWithFlags(&ctx->gathered[k], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&ctx->copied[k], cudaEventDisableTiming));
+    }
+    CK(cudaMallocHost(&ctx->h_flag, 2 * sizeof(int)));
+    ctx->h_flag[0] = ctx->h_flag[1] = 0;
+  }
+  const int k = (int)(ctx->next_ticket & 1);
+  if (!ctx->astage[k]) {
+    // packed xyz (12 B per bead) and the flag word fit in nbead float4
+    ctx->astage[k] = ctx->dalloc<float4>((size_t)ctx->s.nbead + 1);
+    if (!ctx->astage[k]) return ctx->fail(SOP_ERR_ALLOC, "staging buffer allocation failed");
+  }
+  const size_t n3 = 3 * (size_t)ctx->s.nbead;
+  float* packed = reinterpret_cast<float*>(ctx->astage[k]);
+  int* dflag = reinterpret_cast<int*>(packed + n3);
+  // the buffer's previous copy must have left it before the gather refills it
+  CK(cudaStreamWaitEvent(ctx->stream, ctx->copied[k], 0));
+  launch_gather_current(ctx->s, packed, dflag, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ctx->gathered[k], ctx->stream));
+  CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->gathered[k], 0));
+  CK(cudaMemcpyAsync(unc_pos, packed, sizeof(float) * n3, cudaMemcpyDeviceToHost, ctx->copy_stream));
+  CK(cudaMemcpyAsync(ctx->h_flag + k, dflag, sizeof(int), cudaMemcpyDeviceToHost, ctx->copy_stream));
+  CK(cudaEventRecord(ctx->copied[k], ctx->copy_stream));
+  *ticket = ctx->next_ticket++;
+  return SOP_OK;
+}
+
+int sop_download_wait(void* p, long long ticket) {
+  if (!p) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (ticket < 0 || ticket >= ctx->next_ticket || !ctx->copy_stream)
+    return ctx->fail(SOP_ERR_ARG, "no such download");
+  // a buffer's event is re-recorded by the download two tickets later, whose
+  // copy ends after this one's: waiting on it is never too early
+  const int k = (int)(ticket & 1);
+  CK(cudaEventSynchronize(ctx->copied[k]));
+  if (ctx->h_flag[k] & FLAG_NL_OVERFLOW)
+    return ctx->fail(SOP_ERR_CAPACITY,
+                     "the neighbour lists overflowed before the download: sop_sync re-runs the "
+                     "frozen steps, then download again");
   return SOP_OK;
 }
 

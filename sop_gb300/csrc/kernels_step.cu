@@ -511,8 +511,9 @@ __global__ void k_observables_final(const double* __restrict__ part, int nblocks
 
 // Every bead's current unwrapped coordinates (each molecule at its own step
 // parity) in bead-id order, for one device-to-host copy.
-__global__ void k_gather_current(DevSys s, float* __restrict__ out) {
+__global__ void k_gather_current(DevSys s, float* __restrict__ out, int* __restrict__ flag_out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0 && flag_out) *flag_out = *s.flags;  // a frozen context's coordinates are stale
   if (i >= s.nbead) return;
   int m = s.mol_of[i];
   const float4 x = m < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : s.x[(int)(s.mol_step[m] & 1)][i];
@@ -557,8 +558,8 @@ void launch_step(const DevSys& s, int G, bool split, int koff, bool step, cudaSt
   }
 }
 
-void launch_gather_current(const DevSys& s, float* out, cudaStream_t st) {
-  k_gather_current<<<cdiv(s.nbead, 256), 256, 0, st>>>(s, out);
+void launch_gather_current(const DevSys& s, float* out, int* flag_out, cudaStream_t st) {
+  k_gather_current<<<cdiv(s.nbead, 256), 256, 0, st>>>(s, out, flag_out);
 }
 
 void launch_advance(const DevSys& s, int steps, cudaStream_t st) {

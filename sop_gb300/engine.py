@@ -124,6 +124,8 @@ def lib() -> ctypes.CDLL:
             "sop_download_list": (I, [V, I, I, LL, V, V, V, PLL]),
             "sop_list_sizes": (I, [V, V]),
             "sop_download_all": (I, [V, V]),
+            "sop_download_all_async": (I, [V, V, PLL]),
+            "sop_download_wait": (I, [V, LL]),
             "sop_energy": (I, [V, I, V]),
             "sop_observables": (I, [V, I, V]),
             "sop_molecule_status": (I, [V, I, ctypes.POINTER(I), PLL]),
@@ -305,6 +307,22 @@ class Engine:
         assert out.dtype == np.float32 and out.flags.c_contiguous and out.size == 3 * total
         self._check(lib().sop_download_all(self.h, _p(out)), self.h)
         return out
+
+    def download_all_async(self, out: np.ndarray) -> int:
+        """Queues the copy of every bead's coordinates (as download_all, at the
+        point the queued work will have reached) into `out` and returns a
+        ticket for download_wait.  `out` should be page-locked (the call then
+        returns at once) and must stay alive until the wait."""
+        total = sum(m.n for m in self.mols)
+        assert out.dtype == np.float32 and out.flags.c_contiguous and out.size == 3 * total
+        t = ctypes.c_longlong()
+        self._check(lib().sop_download_all_async(self.h, _p(out), ctypes.byref(t)), self.h)
+        self._inflight = getattr(self, "_inflight", {})
+        self._inflight[t.value % 2] = out   # keeps the destination alive
+        return t.value
+
+    def download_wait(self, ticket: int) -> None:
+        self._check(lib().sop_download_wait(self.h, int(ticket)), self.h)
 
     def energy(self, mol: int = 0) -> np.ndarray:
         t = np.zeros(5, np.float64)

@@ -387,3 +387,46 @@ def test_download_all_matches_per_molecule_downloads():
     each = np.concatenate([e.download(k)["unc_pos"] for k in range(len(mols))])
     e.close()
     np.testing.assert_array_equal(allx, each)
+
+
+def test_download_all_async_overlaps_and_matches_blocking_downloads():
+    """sop_download_all_async: queued between queued steps, each download
+    holds the coordinates of the point in the queue where it was issued (the
+    same bits as a blocking download there), with two downloads in flight
+    and a third reusing the first one's buffer; bad tickets are refused."""
+    torch = pytest.importorskip("torch")
+    mols = [mol_of(128, 0), mol_of(4000, 1), mol_of(300, 5)]
+    total = sum(m.n for m in mols)
+
+    def make():
+        e = engine.Engine(engine.baseline_params())
+        for k, m in enumerate(mols):
+            e.add(m, m.xyz, T=0.6, traj=k)
+        e.commit()
+        return e
+
+    ref = make()
+    want = []
+    for n in (10, 7, 13, 10):
+        ref.step(n)
+        want.append(ref.download_all().copy())
+    ref.close()
+
+    e = make()
+    bufs = [torch.empty((total, 3), dtype=torch.float32, pin_memory=True).numpy() for _ in range(4)]
+    tickets = []
+    for k, n in enumerate((10, 7, 13, 10)):
+        e.step_async(n)
+        tickets.append(e.download_all_async(bufs[k]))
+    got = []
+    for t, b in zip(tickets, bufs):
+        e.download_wait(t)
+        got.append(b.copy())
+    e.sync()
+    with pytest.raises(engine.SopError) as ei:
+        e.download_wait(len(tickets))   # never issued
+    assert ei.value.code == 1
+    e.close()
+    assert tickets == [0, 1, 2, 3]
+    for g, w in zip(got, want):
+        np.testing.assert_array_equal(g, w)
