@@ -9,14 +9,15 @@
 //      image matters, fall back to index-chunked cells that scan all pairs)
 //                                                                k_grid, k_grid_base
 //   3. counting sort of beads into cells (own scan), cells sorted by bead id
-//      so every later order is deterministic                     k_assign, scan, k_scatter, k_cellsort
+//      so every later order is deterministic, coordinates staged in that
+//      order                             k_assign, scan, k_scatter, k_cellsort, k_stage_xs
 //   4. 8 lanes per bead in cell order: the bead against the beads of the
 //      cell rows within S along each axis, culled to its own cut-off sphere;
 //      predicate = the reference's FP32 host filter (d^2 < rcut^2, |i-j| > 2,
 //      not native); one pass writes fixed-stride rows (overflow: regrow) k_nl
 //   The attractive neighbour list filters each bead's native row (k_assign).
-// Pair list (every nplup steps): eight lanes per bead compact its
-// neighbour-list row in place order (k_pl).
+// Pair list (every nplup steps): eight lanes per bead, beads in chain order,
+// compact its neighbour-list row in row order (k_pl).
 #include "sop_dev.cuh"
 
 namespace sop {
@@ -295,27 +296,30 @@ __global__ void k_scatter(DevSys s) {
   s.sorted[s.cell_start[c] + s.bead_slot[i]] = i;
 }
 
-// Per cell: sort its beads by id (fixes every downstream order), then stage
-// coordinates in cell order with w = (id << 2) | type.
-__global__ void k_cellsort(DevSys s, int koff, const int* __restrict__ cells_total) {
+// Per cell: sort its beads by id (fixes every downstream order).  Cells hold
+// a handful of beads, so one thread's insertion sort is short.
+__global__ void k_cellsort(DevSys s, const int* __restrict__ cells_total) {
   long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= *cells_total) return;
   int cnt = s.cell_cnt[c];
   if (cnt == 0) return;
-  int st = s.cell_start[c];
-  int* b = s.sorted + st;
+  int* b = s.sorted + s.cell_start[c];
   for (int a = 1; a < cnt; ++a) {
     int v = b[a], k = a;
     while (k > 0 && b[k - 1] > v) { b[k] = b[k - 1]; --k; }
     b[k] = v;
   }
-  for (int a = 0; a < cnt; ++a) {
-    int i = b[a];
-    int m = s.mol_of[i];
-    float4 x = xbuf(s, m, koff)[i];
-    x.w = __int_as_float((i << 2) | type_of(x));
-    s.xs[st + a] = x;
-  }
+}
+
+// Coordinates staged in cell order, w = (id << 2) | type: a thread per
+// position, so the gathers are independent.
+__global__ void k_stage_xs(DevSys s, int koff) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= s.cell_start[s.cell_cap]) return;  // beads that were binned
+  const int i = s.sorted[k];
+  float4 x = xbuf(s, s.mol_of[i], koff)[i];
+  x.w = __int_as_float((i << 2) | type_of(x));
+  s.xs[k] = x;
 }
 
 constexpr int kNatRegs = 16;  // native partners held in registers (the rest are read)
@@ -444,7 +448,7 @@ __global__ void __launch_bounds__(256) k_nl(DevSys s) {
 // neighbour list.
 constexpr int kPlLanes = 8;   // lanes per bead in the pair-list rebuild
 template <bool UNI>
-__global__ void __launch_bounds__(256) k_pl(DevSys s, int koff) {
+__global__ void __launch_bounds__(256, 5) k_pl(DevSys s, int koff) {  // 48 registers: 5 blocks per SM
   pdl_wait();
   pdl_release();
   const int wl = threadIdx.x & 31;
@@ -562,7 +566,8 @@ static void launch_binning(const DevSys& s, const NLScratch& w, int koff, int at
   k_assign<<<cdiv(s.nlive, T), T, 0, st>>>(s, koff, att);
   launch_scan(s.cell_cnt, s.cell_cap, s.cell_start, w.block_sums, st);
   k_scatter<<<cdiv(s.nlive, T), T, 0, st>>>(s);
-  k_cellsort<<<cdiv(s.cell_cap, T), T, 0, st>>>(s, koff, w.cells_total);
+  k_cellsort<<<cdiv(s.cell_cap, T), T, 0, st>>>(s, w.cells_total);
+  k_stage_xs<<<cdiv(s.nlive, T), T, 0, st>>>(s, koff);
 }
 
 // Full neighbour-list rebuild from the coordinates at step mol_step + koff.
