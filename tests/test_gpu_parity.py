@@ -99,6 +99,72 @@ def test_forces_per_contact_epsilon():
     assert force_error(f, fo) <= FORCE_TOL
 
 
+def test_rep6_forces_and_energy_vs_fp64():
+    """The pure 6-power repulsion (rep6 = 1; the reference's form is 12+6):
+    forces within 1e-5 and energies within 2e-5 of FP64."""
+    mol = mol_of(4000, 1)
+    x = perturbed(mol, 0.25, 13)
+    with engine.plain(mol, x, params("absolute", rep6=1)) as e:
+        e.set_noise(np.zeros((mol.n, 3), np.float32))
+        e.force_eval()
+        assert e.status(0)[0] == 0
+        f = e.download()["force"]
+        t = e.energy()
+        pai, paj, _ = e.list_pairs(0, 2)
+        pri, prj, _ = e.list_pairs(0, 3)
+    fo, eo = O.forces_f64(mol, x, att_sel(mol, pai, paj), pri, prj, params={"rep6": 1})
+    assert force_error(f, fo) <= FORCE_TOL
+    np.testing.assert_allclose(t[:4], eo, rtol=2e-5, atol=1e-6)
+    f12, _ = O.forces_f64(mol, x, att_sel(mol, pai, paj), pri, prj)
+    assert force_error(f, f12) > 1e-3   # the flag changes the physics
+
+
+def test_tiny_molecules_beside_a_large_one():
+    """Chains of 3 to 8 beads (no native contacts below 4 beads, no
+    repulsive pairs below 4, chain ends everywhere) batched with a 4000-bead
+    molecule: lists bit-exact, forces within 1e-5 of FP64, and 50 steps
+    without an error flag."""
+    mols = [mol_of(n, 30 + n) for n in (3, 4, 5, 6, 8)] + [mol_of(4000, 1)]
+    p = params("absolute")
+    e = engine.Engine(p)
+    xs = []
+    for k, m in enumerate(mols):
+        x = perturbed(m, 0.1, 40 + k)
+        xs.append(x)
+        e.add(m, x, T=0.6, traj=k)
+    e.commit()
+    e.set_noise(np.zeros((sum(m.n for m in mols), 3), np.float32))
+    e.force_eval()
+    for k, (m, x) in enumerate(zip(mols, xs)):
+        ai, aj, _ = e.list_pairs(k, 0)
+        ri, rj, _ = e.list_pairs(k, 1)
+        pai, paj, _ = e.list_pairs(k, 2)
+        pri, prj, _ = e.list_pairs(k, 3)
+        nl_att, (nri, nrj), pl_att, (opi, opj) = oracle_lists(m, x, p)
+        assert pairset(ai, aj) == pairset(m.nat_i[nl_att], m.nat_j[nl_att])
+        assert pairset(ri, rj) == pairset(nri, nrj)
+        assert pairset(pai, paj) == pairset(m.nat_i[pl_att], m.nat_j[pl_att])
+        assert pairset(pri, prj) == pairset(opi, opj)
+        if m.n < 4:
+            assert len(ri) == 0 and len(m.nat_i) == 0
+        fo, _ = O.forces_f64(m, x, att_sel(m, pai, paj), pri, prj)
+        assert force_error(e.download(k)["force"], fo) <= FORCE_TOL, m.n
+    e.set_noise(None)
+    e.step(50)
+    for k in range(len(mols)):
+        st, n = e.status(k)
+        assert st == 0 and n == 50
+    e.close()
+
+
+def test_commit_without_molecules_is_refused():
+    e = engine.Engine(params("absolute"))
+    with pytest.raises(engine.SopError) as ei:
+        e.commit()
+    assert ei.value.code == 1   # SOP_ERR_ARG
+    e.close()
+
+
 @pytest.mark.parametrize("mode", ["factor", "absolute"])
 def test_energy_vs_fp64(mode):
     mol = mol_of(4000, 1)
