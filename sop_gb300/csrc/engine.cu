@@ -1335,7 +1335,7 @@ static int serve_round(SopCtx* ctx) {
     if (rc) return rc;
     if (resumed) {
       // the job continues at its checkpoint's step: its state and lists come
-      // from the checkpoint, and the beads join the cell order below
+      // from the checkpoint, and the binning below sets the molecule's grid flags
       rc = restore_into(ctx, slot, jb.resume.data(), (long long)jb.resume.size());
       if (rc) return rc;
       jb.resume.clear();
@@ -1959,8 +1959,8 @@ int sop_restore(void* p, int mol, const void* buf, long long size) {
     return ctx->fail(SOP_ERR_ARG, "checkpoint step differs from the context's step");
   rc = restore_into(ctx, mol, static_cast<const char*>(buf), size);
   if (rc) return rc;
-  // refresh the cell order and each molecule's grid flags from the restored
-  // coordinates (binning only: no list changes, no result depends on it)
+  // refresh each molecule's grid flags (and the cell order) from the restored
+  // coordinates: binning only, no list changes
   launch_rebin(ctx->s, ctx->w, ctx->stream);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));

@@ -553,9 +553,10 @@ struct NLScratch {
   int* cells_total;  // one int: cells in use
 };
 
-// Cell binning of the molecules a rebuild at koff covers (the cell order the
-// step kernel and the pair-list rebuild walk); att = 1 also refreshes the
-// attractive neighbour lists.
+// Cell binning of the molecules a rebuild at koff covers: the cell order the
+// neighbour-list build walks, and each molecule's grid flags (wrap: whether
+// the minimum image can matter), which the step and pair-list kernels read;
+// att = 1 also refreshes the attractive neighbour lists.
 static void launch_binning(const DevSys& s, const NLScratch& w, int koff, int att, cudaStream_t st) {
   const int T = 256;
   k_bbox_reset<<<cdiv(s.nmol, T), T, 0, st>>>(s);
@@ -580,9 +581,10 @@ void launch_nl_rebuild(const DevSys& s, const NLScratch& w, int koff, cudaStream
     k_nl<false><<<cdiv((long long)s.nlive * kNlLanes, T), T, 0, st>>>(s);
 }
 
-// The cell order alone, every list untouched: puts molecules that arrive
-// with their lists (restored from a checkpoint) into the order the step
-// kernel walks.  The order decides no result.
+// The binning alone, every list untouched: molecules that arrive with their
+// lists (restored from a checkpoint) get grid flags from their own
+// coordinates, which the step and pair-list kernels need.  The cell order
+// itself decides no result.
 void launch_rebin(const DevSys& s, const NLScratch& w, cudaStream_t st) {
   launch_binning(s, w, 0, 0, st);
 }
