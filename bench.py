@@ -160,7 +160,8 @@ def whole_job_rate(beads_per_rank: int, md_steps: int, world: int, t_max: float)
 def launches_per_bench_step(p, s0: int, step_kernels: int = 1) -> int:
     """Kernels of the engine in one replay starting after step s0
     (step_kernels: 1 for the one-kernel step, 2 for force + finish)."""
-    nl_kernels = 11    # bbox reset, bbox, grid, grid base, assign, 3 scan, scatter, cellsort, nl
+    nl_kernels = 12    # bbox reset, bbox, grid, grid base, assign, 3 scan, scatter, cellsort,
+                       # stage_xs, nl
     n = 0
     for k in range(MD_STEPS):
         st = s0 + 1 + k
