@@ -514,21 +514,22 @@ __global__ void __launch_bounds__(256, 5) k_pl(DevSys s, int koff) {  // 48 regi
   for (int e0 = 0; e0 < acnt; e0 += kPlLanes) {
     const int e = e0 + lane;
     bool pass = false;
-    int idx = 0, j = 0;
+    int j = 0;
+    float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
     if (e < acnt) {
-      idx = s.nl_att_e[row.x + e];
+      const int idx = s.nl_att_e[row.x + e];
+      // the contact's partner, cut-off and parameters in one round of loads
       j = s.nat_j[idx];
-      float4 xj = X[j];
+      const float rc2 = s.nat_rc2[idx].y;
+      q = s.nat_par[idx];
+      const float4 xj = X[j];
       float dx = __fsub_rn(xj.x, xi.x), dy = __fsub_rn(xj.y, xi.y),
             dz = __fsub_rn(xj.z, xi.z);
       if (wrap) min_image3(dx, dy, dz, boxl);
-      pass = d2_exact(dx, dy, dz) < s.nat_rc2[idx].y;
+      pass = d2_exact(dx, dy, dz) < rc2;
     }
     const unsigned mask = (__ballot_sync(gmask, pass) >> (wl & ~(kPlLanes - 1))) & ((1u << kPlLanes) - 1u);
-    if (pass) {
-      float4 q = s.nat_par[idx];
-      s.pl_att[row.x + ka + __popc(mask & lt)] = make_float4(__int_as_float(j), q.x, q.y, q.z);
-    }
+    if (pass) s.pl_att[row.x + ka + __popc(mask & lt)] = make_float4(__int_as_float(j), q.x, q.y, q.z);
     ka += __popc(mask);
   }
   if (lane == 0) s.pl_att_cnt[i] = ka;
