@@ -9,6 +9,7 @@
 // per-step loop body of underdamped_ctrl (sop.cu:197-243).
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -17,6 +18,7 @@
 #include <map>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "sop_dev.cuh"
@@ -657,28 +659,11 @@ struct Staged {
   std::vector<long long> step0;
   std::vector<MolConst> mc;
   long long beads() const { return (long long)x0.size(); }
-  // appends `t` if its ranges follow on from these; false otherwise
-  bool append(Staged& t) {
-    if (mc.empty()) {
-      *this = std::move(t);
-      return true;
-    }
-    if (t.o != o + beads() || t.ob != ob + (long long)bj.size() || t.oa != oa + (long long)aj.size() ||
-        t.on != on + (long long)nj.size() || t.slot0 != slot0 + (int)mc.size())
-      return false;
-    auto cat = [](auto& a, auto& b) { a.insert(a.end(), b.begin(), b.end()); };
-    cat(brow, t.brow); cat(arow, t.arow); cat(nrow, t.nrow);
-    cat(bj, t.bj); cat(aj, t.aj); cat(nj, t.nj); cat(molof, t.molof);
-    cat(br, t.br); cat(np, t.np); cat(x0, t.x0); cat(p0, t.p0); cat(v0, t.v0);
-    cat(nr, t.nr); cat(step0, t.step0); cat(mc, t.mc);
-    return true;
-  }
 };
 
-// Takes pool ranges for molecule `hm` in slot `slot` and builds its device
-// rows on the host.  SOP_ERR_CAPACITY when the pools cannot hold it.
-int stage_install(SopCtx* ctx, int slot, HostMol& hm, long long step0, Staged& S) {
-  const sop_params& P = ctx->P;
+// Takes pool ranges for molecule `hm` in slot `slot`.  SOP_ERR_CAPACITY when
+// the pools cannot hold it.
+int take_ranges(SopCtx* ctx, int slot, HostMol& hm) {
   const long long nb2 = 2LL * (long long)hm.bi.size(), na2 = 2LL * (long long)hm.ai.size(),
                   nn2 = 2LL * (long long)hm.ni.size();
   long long b0 = ctx->bead_alloc.alloc(hm.n);
@@ -696,62 +681,93 @@ int stage_install(SopCtx* ctx, int slot, HostMol& hm, long long step0, Staged& S
   hm.start = (int)b0;
   hm.slot = slot;
   hm.off_b = ob; hm.off_a = oa; hm.off_n = on;
-  const int n = hm.n, o = (int)b0;
-  S.o = b0; S.ob = ob; S.oa = oa; S.on = on; S.slot0 = slot;
-  S.brow.assign(n, int2{}); S.arow.assign(n, int2{}); S.nrow.assign(n, int2{});
+  return SOP_OK;
+}
+
+// Builds molecule `hm`'s device rows (its ranges already taken) into S,
+// whose arrays start at pool positions S.o / S.ob / S.oa / S.on and are
+// sized to hold it; k is its index among S's molecules.  Touches only the
+// molecule's own part of S, so molecules may be built concurrently.
+void fill_rows(const SopCtx* ctx, const HostMol& hm, int k, long long step0, Staged& S) {
+  const sop_params& P = ctx->P;
+  const int n = hm.n, o = hm.start;
+  const long long ob = hm.off_b, oa = hm.off_a, on = hm.off_n;
+  int2* brow = S.brow.data() + (o - S.o);
+  int2* arow = S.arow.data() + (o - S.o);
+  int2* nrow = S.nrow.data() + (o - S.o);
   std::vector<int> cnt_b(n, 0), cnt_a(n, 0), cnt_n(n, 0);
-  for (size_t k = 0; k < hm.bi.size(); ++k) { cnt_b[hm.bi[k]]++; cnt_b[hm.bj[k]]++; }
-  for (size_t k = 0; k < hm.ai.size(); ++k) { cnt_a[hm.ai[k]]++; cnt_a[hm.ak[k]]++; }
-  for (size_t k = 0; k < hm.ni.size(); ++k) { cnt_n[hm.ni[k]]++; cnt_n[hm.nj[k]]++; }
+  for (size_t q = 0; q < hm.bi.size(); ++q) { cnt_b[hm.bi[q]]++; cnt_b[hm.bj[q]]++; }
+  for (size_t q = 0; q < hm.ai.size(); ++q) { cnt_a[hm.ai[q]]++; cnt_a[hm.ak[q]]++; }
+  for (size_t q = 0; q < hm.ni.size(); ++q) { cnt_n[hm.ni[q]]++; cnt_n[hm.nj[q]]++; }
   {
     int eb = (int)ob, ea = (int)oa, en = (int)on;
     for (int i = 0; i < n; ++i) {
-      S.brow[i] = make_int2(eb, 0); eb += cnt_b[i];
-      S.arow[i] = make_int2(ea, 0); ea += cnt_a[i];
-      S.nrow[i] = make_int2(en, 0); en += cnt_n[i];
+      brow[i] = make_int2(eb, 0); eb += cnt_b[i];
+      arow[i] = make_int2(ea, 0); ea += cnt_a[i];
+      nrow[i] = make_int2(en, 0); en += cnt_n[i];
     }
   }
-  S.bj.assign(nb2, 0); S.aj.assign(na2, 0); S.nj.assign(nn2, 0); S.molof.assign(n, slot);
-  S.br.assign(nb2, 0.f);
-  S.np.assign(nn2, float4{});
-  S.nr.assign(nn2, float2{});
   auto put_b = [&](int i, int j, float r0) {
-    int e = S.brow[i].x + S.brow[i].y++ - (int)ob;
+    const long long e = brow[i].x + brow[i].y++ - S.ob;
     S.bj[e] = o + j; S.br[e] = r0;
   };
-  auto put_a = [&](int i, int j) { S.aj[S.arow[i].x + S.arow[i].y++ - (int)oa] = o + j; };
+  auto put_a = [&](int i, int j) { S.aj[arow[i].x + arow[i].y++ - S.oa] = o + j; };
   auto put_n = [&](int i, int j, float r0, float ef, float ee) {
-    int e = S.nrow[i].x + S.nrow[i].y++ - (int)on;
+    const long long e = nrow[i].x + nrow[i].y++ - S.on;
     S.nj[e] = o + j;
     S.np[e] = make_float4(r0, ef, ee, 0.f);
     S.nr[e] = make_float2(rcut2_of(P.nl_att_fac, P.nl_att_abs, r0),
                           rcut2_of(P.pl_att_fac, P.pl_att_abs, r0));
   };
-  for (size_t k = 0; k < hm.bi.size(); ++k) {
-    put_b(hm.bi[k], hm.bj[k], hm.br0[k]);
-    put_b(hm.bj[k], hm.bi[k], hm.br0[k]);
+  for (size_t q = 0; q < hm.bi.size(); ++q) {
+    put_b(hm.bi[q], hm.bj[q], hm.br0[q]);
+    put_b(hm.bj[q], hm.bi[q], hm.br0[q]);
   }
-  for (size_t k = 0; k < hm.ai.size(); ++k) {
-    put_a(hm.ai[k], hm.ak[k]);
-    put_a(hm.ak[k], hm.ai[k]);
+  for (size_t q = 0; q < hm.ai.size(); ++q) {
+    put_a(hm.ai[q], hm.ak[q]);
+    put_a(hm.ak[q], hm.ai[q]);
   }
-  for (size_t k = 0; k < hm.ni.size(); ++k) {
-    put_n(hm.ni[k], hm.nj[k], hm.nr0[k], hm.neps[k], hm.nepse[k]);
-    put_n(hm.nj[k], hm.ni[k], hm.nr0[k], hm.neps[k], hm.nepse[k]);
+  for (size_t q = 0; q < hm.ni.size(); ++q) {
+    put_n(hm.ni[q], hm.nj[q], hm.nr0[q], hm.neps[q], hm.nepse[q]);
+    put_n(hm.nj[q], hm.ni[q], hm.nr0[q], hm.neps[q], hm.nepse[q]);
   }
-  S.x0.assign(n, float4{}); S.p0.assign(n, float4{}); S.v0.assign(n, float4{});
+  const std::vector<float>& pp = hm.pos.empty() ? hm.unc : hm.pos;
   for (int i = 0; i < n; ++i) {
-    int t = hm.types.empty() ? 1 : hm.types[i];
-    S.x0[i] = make_float4(hm.unc[3 * i], hm.unc[3 * i + 1], hm.unc[3 * i + 2], bits_f(t));
-    const std::vector<float>& pp = hm.pos.empty() ? hm.unc : hm.pos;
-    S.p0[i] = make_float4(pp[3 * i], pp[3 * i + 1], pp[3 * i + 2], 0.f);
-    S.v0[i] = hm.vel.empty() ? make_float4(0.f, 0.f, 0.f, 0.f)
+    const size_t d = (size_t)(o - S.o) + i;
+    const int t = hm.types.empty() ? 1 : hm.types[i];
+    S.molof[d] = hm.slot;
+    S.x0[d] = make_float4(hm.unc[3 * i], hm.unc[3 * i + 1], hm.unc[3 * i + 2], bits_f(t));
+    S.p0[d] = make_float4(pp[3 * i], pp[3 * i + 1], pp[3 * i + 2], 0.f);
+    S.v0[d] = hm.vel.empty() ? make_float4(0.f, 0.f, 0.f, 0.f)
                              : make_float4(hm.vel[3 * i], hm.vel[3 * i + 1], hm.vel[3 * i + 2], 0.f);
   }
-  MolConst mcst = make_const(P, hm);
-  ctx->mc[slot] = mcst;
-  S.mc.assign(1, mcst);
-  S.step0.assign(1, step0);
+  S.mc[k] = make_const(P, hm);
+  S.step0[k] = step0;
+}
+
+// Sizes S for `beads` beads, `b2` / `a2` / `n2` bond / angle / native entries
+// and `nm` molecules starting at the given pool positions and slot.
+void size_staged(Staged& S, long long o, long long ob, long long oa, long long on, int slot0,
+                 long long beads, long long b2, long long a2, long long n2, int nm) {
+  S.o = o; S.ob = ob; S.oa = oa; S.on = on; S.slot0 = slot0;
+  S.brow.assign(beads, int2{}); S.arow.assign(beads, int2{}); S.nrow.assign(beads, int2{});
+  S.molof.assign(beads, 0);
+  S.x0.assign(beads, float4{}); S.p0.assign(beads, float4{}); S.v0.assign(beads, float4{});
+  S.bj.assign(b2, 0); S.br.assign(b2, 0.f);
+  S.aj.assign(a2, 0);
+  S.nj.assign(n2, 0); S.np.assign(n2, float4{}); S.nr.assign(n2, float2{});
+  S.mc.assign(nm, MolConst{});
+  S.step0.assign(nm, 0);
+}
+
+// One molecule: its ranges and rows, staged on the host.
+int stage_install(SopCtx* ctx, int slot, HostMol& hm, long long step0, Staged& S) {
+  int rc = take_ranges(ctx, slot, hm);
+  if (rc) return rc;
+  size_staged(S, hm.start, hm.off_b, hm.off_a, hm.off_n, slot, hm.n, 2LL * (long long)hm.bi.size(),
+              2LL * (long long)hm.ai.size(), 2LL * (long long)hm.ni.size(), 1);
+  fill_rows(ctx, hm, 0, step0, S);
+  ctx->mc[slot] = S.mc[0];
   return SOP_OK;
 }
 
@@ -863,20 +879,29 @@ int commit(SopCtx* ctx) {
   for (auto& m : ctx->mols)
     for (int t : m.types)
       if (t != 1) ctx->s.uniform_type = 0;
-  // every molecule's rows staged on the host, then one copy per array (the
-  // pools are fresh, so the molecules' ranges follow one another)
-  Staged all;
-  for (int k = 0; k < (int)ctx->mols.size(); ++k) {
+  // every molecule's ranges taken in id order (the pools are fresh, so they
+  // follow one another from 0), its rows built on the host by a pool of
+  // threads, then one copy per array
+  const int nm = (int)ctx->mols.size();
+  for (int k = 0; k < nm; ++k) {
     ctx->free_slots.pop_back();  // slots handed out in id order
-    Staged one;
-    rc = stage_install(ctx, k, ctx->mols[k], 0, one);
+    rc = take_ranges(ctx, k, ctx->mols[k]);
     if (rc) return ctx->fail(rc, "pool sizing error");
-    if (!all.append(one)) {
-      rc = upload_staged(ctx, all);
-      if (rc) return rc;
-      all = std::move(one);
-    }
   }
+  Staged all;
+  size_staged(all, 0, 0, 0, 0, 0, c.beads, c.bonds, c.angles, c.natives, nm);
+  {
+    const int nthr = std::max(1, std::min<int>(16, (int)std::thread::hardware_concurrency()));
+    std::atomic<int> next{0};
+    auto work = [&] {
+      for (int k = next++; k < nm; k = next++) fill_rows(ctx, ctx->mols[k], k, 0, all);
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nthr && t < nm; ++t) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+  }
+  for (int k = 0; k < nm; ++k) ctx->mc[k] = all.mc[k];
   rc = upload_staged(ctx, all);
   if (rc) return rc;
   rc = setup_step0(ctx);
