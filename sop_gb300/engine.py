@@ -177,7 +177,13 @@ def baseline_params(**kw) -> Params:
 
 
 def _p(a):
-    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+    """The address of an array's data (None for None)."""
+    if a is None:
+        return None
+    try:  # the buffer protocol: about a third of the cost of .ctypes
+        return ctypes.c_void_p(ctypes.addressof(ctypes.c_char.from_buffer(a)))
+    except (TypeError, ValueError, BufferError):  # read-only or empty arrays
+        return ctypes.c_void_p(a.ctypes.data)
 
 
 class Engine:
