@@ -5,8 +5,9 @@
 // Neighbour list (every nnlup steps):
 //   1. per-molecule bounding box of the coordinates             k_bbox
 //   2. per-molecule cell grid (cell edge rc/S, S=1..3 chosen so a cell holds
-//      ~4 beads; molecules whose extent + rc reaches boxl, where the minimum
-//      image matters, fall back to index-chunked cells that scan all pairs)
+//      ~4 beads; S=1..4 and ~1 bead from 10,000 beads up; molecules whose
+//      extent + rc reaches boxl, where the minimum image matters, fall back
+//      to index-chunked cells that scan all pairs)
 //                                                                k_grid, k_grid_base
 //   3. counting sort of beads into cells (own scan), cells sorted by bead id
 //      so every later order is deterministic, coordinates staged in that
@@ -193,8 +194,13 @@ __global__ void k_grid(DevSys s, int* __restrict__ ncell, int koff) {
   } else {
     float vol = fmaxf((ext[0] + 1.0f) * (ext[1] + 1.0f) * (ext[2] + 1.0f), 1.0f);
     float rho = (float)n / vol;
-    int S = (int)floorf(rc * cbrtf(rho * 0.25f));
-    S = S < 1 ? 1 : (S > 3 ? 3 : S);
+    // about 4 beads per cell (S <= 3); a molecule of 10,000 beads or more
+    // scans enough cells per bead that finer ones (about 1 bead, S <= 4) cull
+    // more candidates than they add rows
+    const bool big = n >= 10000;
+    const int smax = big ? 4 : 3;
+    int S = (int)floorf(rc * cbrtf(rho * (big ? 1.0f : 0.25f)));
+    S = S < 1 ? 1 : (S > smax ? smax : S);
     float cs = rc * 1.0001f / (float)S + 1.0e-4f;
     long long cap = n * 2 > 64 ? (long long)n * 2 : 64;
     for (int iter = 0; iter < 8; ++iter) {
