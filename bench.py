@@ -75,9 +75,10 @@ def measured_peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def profile_traffic() -> float | None:
-    """DRAM bytes per launch of the step kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "step_kernel_ensemble.md")
+def profile_traffic(workload: str = "ensemble") -> float | None:
+    """DRAM bytes per launch of the step kernel from the committed ncu summary
+    of that workload (None when there is none)."""
+    p = os.path.join(ROOT, "profiles", f"step_kernel_{workload}.md")
     try:
         for line in open(p):
             if line.strip().startswith("traffic_bytes_per_launch:"):
@@ -304,7 +305,8 @@ def plain_one(args, local: int) -> None:
     torch.cuda.set_device(local)
     nbead, seed, eps = PLAIN[args.workload]
     mol = system.generate(nbead, seed, eps)
-    p = engine.baseline_params(device=local, graph_steps=MD_STEPS)
+    p = engine.baseline_params(device=local, graph_steps=MD_STEPS, lanes_per_bead=args.lanes,
+                               step_split=args.form)
     e = engine.plain(mol, mol.xyz, p, T=0.6)
     stream = torch.cuda.ExternalStream(e.stream(), device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -391,7 +393,7 @@ def plain_one(args, local: int) -> None:
                        "md_steps_per_bench_step": MD_STEPS,
                        "l2": "flushed before every timed step (256 MiB write)"},
             "roofline": {"bound": "hbm", "achieved": s0["achieved_gbs"], "peak": peak,
-                         "unit": "GB/s", "frac": s0["frac"], "traffic": None,
+                         "unit": "GB/s", "frac": s0["frac"], "traffic": profile_traffic(args.workload),
                          "kernel": names[0], "peak_source": peak_kind},
             "cpu_baseline": cpu, "tuning": tuning,
             "stages": stages, "lists": ls, "gpu_launches": int(n_launch), "clocks": clk.summary()}
