@@ -281,6 +281,8 @@ struct SopCtx {
 
 static SopCtx* C(void* p) { return static_cast<SopCtx*>(p); }
 
+int grow_nl_keep(SopCtx* ctx, long long stride);
+
 #define CK(call)                                         \
   do {                                                   \
     cudaError_t e_ = (call);                             \
@@ -358,12 +360,15 @@ int alloc_nl(SopCtx* ctx, long long stride) {
 }
 
 // After a neighbour-list overflow: regrow the row stride to 1.25x the longest
-// row the rebuild needed and clear the flag.  The stream must be idle.
+// row the rebuild needed and clear the flag.  The rows are kept: the rebuild
+// that runs again rewrites those of the molecules it covers, and a molecule
+// it does not cover (finished or stopped) keeps the lists of its last step,
+// which its energy is evaluated on.  The stream must be idle.
 int grow_nl(SopCtx* ctx) {
   int maxrow = 0;
   CK(cudaMemcpy(&maxrow, ctx->s.nl_maxrow, sizeof(int), cudaMemcpyDeviceToHost));
   long long stride = std::max<long long>(ctx->s.nl_stride + 32, (long long)maxrow * 5 / 4 + 32);
-  int rc = alloc_nl(ctx, stride);
+  int rc = grow_nl_keep(ctx, stride);
   if (rc) return rc;
   CK(cudaMemsetAsync(ctx->s.nl_maxrow, 0, sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(ctx->s.flags, 0, sizeof(int), ctx->stream));
@@ -371,10 +376,12 @@ int grow_nl(SopCtx* ctx) {
 }
 
 // Neighbour-list rebuild that regrows the rows on overflow and rebuilds
-// again.  Synchronous.
-int nl_rebuild_checked(SopCtx* ctx, int koff) {
+// again; only_mol >= 0 rebuilds that molecule's lists alone.  Synchronous.
+int nl_rebuild_checked(SopCtx* ctx, int koff, int only_mol = -1) {
   for (int attempt = 0; attempt < 4; ++attempt) {
-    launch_nl_rebuild(ctx->s, ctx->w, koff, ctx->stream);
+    DevSys s = ctx->s;  // re-read: a regrow changes the rows
+    s.only_mol = only_mol;
+    launch_nl_rebuild(s, ctx->w, koff, ctx->stream);
     CK(cudaGetLastError());
     int flags = 0;
     CK(cudaMemcpyAsync(&flags, ctx->s.flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -551,6 +558,7 @@ int alloc_pools(SopCtx* ctx, const Caps& c) {
   const size_t nb = (size_t)c.beads, nm = (size_t)c.mols;
   s.nbead = (int)c.beads;
   s.nlive = s.nbead;
+  s.only_mol = -1;
   s.nmol = (int)c.mols;
   for (int b = 0; b < 2; ++b) {
     s.x[b] = ctx->dalloc<float4>(nb);
@@ -1584,10 +1592,14 @@ int sop_upload_state(void* p, int mol, const float* pos, const float* unc_pos, c
     for (int i = 0; i < hm.n; ++i) buf[i] = make_float4(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], 0.f);
     CK(cudaMemcpy(ctx->s.v + hm.start, buf.data(), sizeof(float4) * hm.n, cudaMemcpyHostToDevice));
   }
-  rc = nl_rebuild_checked(ctx, -1);
+  // the lists of this molecule alone: the others keep theirs (built from
+  // their own step's coordinates; buffer step - 1 holds their look-ahead)
+  rc = nl_rebuild_checked(ctx, -1, mol);
   if (rc) return rc;
-  launch_pl_rebuild(ctx->s, -1, ctx->stream);
-  force_eval_async(ctx);
+  DevSys one = ctx->s;
+  one.only_mol = mol;
+  launch_pl_rebuild(one, -1, ctx->stream);
+  force_eval_async(ctx);  // every molecule: the same forces again for the others
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
   return SOP_OK;

@@ -122,6 +122,7 @@ __global__ void k_bbox_reset(DevSys s) {
 // lists of its last step, as the reference's loop ends there.
 __device__ __forceinline__ bool mol_listed(const DevSys& s, int m, int koff) {
   if (m < 0) return false;
+  if (s.only_mol >= 0 && m != s.only_mol) return false;  // its lists and grid stay
   const MolConst& mc = s.mol[m];
   return mc.active && s.mol_status[m] == 0 &&
          !(mc.nsteps >= 0 && s.mol_step[m] + koff >= mc.nsteps);
@@ -161,6 +162,10 @@ __global__ void k_bbox(DevSys s, int koff) {
 __global__ void k_grid(DevSys s, int* __restrict__ ncell, int koff) {
   int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= s.nmol) return;
+  if (s.only_mol >= 0 && m != s.only_mol) {  // a rebuild of another molecule alone
+    ncell[m] = 0;
+    return;
+  }
   MolGrid g = {};
   int n = s.mol[m].n;
   if (!mol_listed(s, m, koff) || n <= 0) {

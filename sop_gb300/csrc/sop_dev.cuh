@@ -56,6 +56,7 @@ struct MolGrid {
 struct DevSys {
   int nbead, nmol;
   int nlive;                    // bead slots the per-step kernels cover; every slot past it is free
+  int only_mol;                 // >= 0: a list rebuild covers this molecule alone (a state upload)
   float boxl;
   float eps_rep;
   int rep6;

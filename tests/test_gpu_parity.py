@@ -296,6 +296,43 @@ def test_deterministic_and_graph_equals_eager():
         np.testing.assert_array_equal(outs[0][k], outs[2][k])
 
 
+def test_state_upload_touches_only_its_molecule():
+    """sop_upload_state rebuilds the lists of the molecule it loads and no
+    other: a finished molecule keeps the lists of its last step (its energy
+    is evaluated on them) and a running one continues bit-identically to a
+    run alone, also when the upload's neighbour list overflows the row
+    stride and the rows regrow."""
+    a, b, c = mol_of(128, 0), mol_of(4000, 1), mol_of(300, 5)
+    p = engine.baseline_params(boxl=40000.0)
+    e = engine.Engine(p)
+    e.add(a, a.xyz, T=0.6, traj=0, nsteps=20)
+    e.add(b, b.extended_xyz(), T=0.6, traj=1)
+    e.add(c, c.xyz, T=0.7, traj=2)
+    e.commit()
+    e.step(30)
+    assert e.status(0)[1] == 20 and e.status(1) == (0, 30)
+    before = [e.energy(0), *e.list_pairs(0, 1), *e.list_pairs(0, 3), *e.list_pairs(2, 3)]
+    bytes0 = e.memory(0)[0]
+    e.upload_state(1, b.xyz)          # the folded structure: rows several times longer
+    assert e.memory(0)[0] > bytes0    # the rows regrew
+    after = [e.energy(0), *e.list_pairs(0, 1), *e.list_pairs(0, 3), *e.list_pairs(2, 3)]
+    for x, y in zip(after, before):
+        np.testing.assert_array_equal(x, y)
+    _, (nri, nrj), _, (opi, opj) = oracle_lists(b, b.xyz, p, 40000.0)
+    ri, rj, _ = e.list_pairs(1, 1)
+    pri, prj, _ = e.list_pairs(1, 3)
+    assert pairset(ri, rj) == pairset(nri, nrj)
+    assert pairset(pri, prj) == pairset(opi, opj)
+    e.step(40)
+    mixed = e.download(2)
+    e.close()
+    with engine.plain(c, c.xyz, p, T=0.7, traj=2) as alone:
+        alone.step(70)
+        ref = alone.download()
+    for k in ("unc_pos", "vel", "force"):
+        np.testing.assert_array_equal(mixed[k], ref[k])
+
+
 @pytest.mark.parametrize("boxl", [40000.0, 500.0])
 def test_extended_chain_lists(boxl):
     """Extended start: with a large box the cell grid is a long row; with the
