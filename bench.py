@@ -77,7 +77,9 @@ def measured_peaks() -> tuple[float, str]:
 
 def profile_traffic(workload: str = "ensemble") -> float | None:
     """DRAM bytes per launch of the step kernel from the committed ncu summary
-    of that workload (None when there is none)."""
+    of that workload (None when there is none).  A profile figure: ncu's
+    dram__bytes_read.sum + dram__bytes_write.sum of one capture of the same
+    kernel on the same workload, not measured during this run."""
     p = os.path.join(ROOT, "profiles", f"step_kernel_{workload}.md")
     try:
         for line in open(p):
@@ -219,34 +221,47 @@ def cpu_baseline(mols, ts, seconds_target: float = 15.0) -> dict:
 
 
 SERVED_RATE = 200.0          # jobs/s (Poisson)
-SERVED_SECONDS = 1.0         # arrival window
-SERVED_STEPS = (2e2, 2e4)    # the served stream's step range [1e4, 1e6] scaled by 1/50
-SERVED_BUDGET = 16 << 30     # device bytes for coordinates, velocities, topology, lists
+SERVED_SECONDS = 60.0        # arrival window
+STEP_SCALE = 50              # steps log-uniform [1e4, 1e6] scaled by 1/STEP_SCALE
+SERVED_STEPS = (1e4 / STEP_SCALE, 1e6 / STEP_SCALE)
+SERVED_BUDGET = 150 * 10**9  # device bytes for coordinates, velocities, topology, lists
 SERVED_BOXL = 1.0e6          # holds a fully extended 20,000-bead chain without self-images
+PLAIN_EVERY = 20             # every 20th job (5%) also runs alone on the plain path
 
 
 def served_stream(local: int) -> dict:
-    """Continuous batching on a Poisson request stream, then the same jobs'
-    plain-path speed (a sample run one at a time)."""
+    """Continuous batching on the Poisson request stream: jobs are submitted at
+    their arrival times (structures generated ahead by a pool of host threads),
+    admitted by the HBM budget, retired when done; then every PLAIN_EVERY-th
+    job again alone on the plain path."""
     from sop_gb300 import engine
     req = system.request_stream(SERVED_RATE, SERVED_SECONDS, (50, 20000), SERVED_STEPS,
                                 (0.5, 0.8), seed=5)
     njob = len(req["n"])
-    mols = [system.generate(int(n), 100000 + k) for k, n in enumerate(req["n"])]
-    xyz = [m.extended_xyz() if req["extended"][k] else m.xyz for k, m in enumerate(mols)]
+
+    def make(k):
+        m = system.generate(int(req["n"][k]), 100000 + k)
+        return m, (m.extended_xyz() if req["extended"][k] else m.xyz)
+
     p = engine.baseline_params(device=local, boxl=SERVED_BOXL)
     lat, work, statuses = {}, 0, []
+    gen = ThreadPoolExecutor(max(2, min(8, (os.cpu_count() or 4) // 2)))
+    futs = [gen.submit(make, k) for k in range(njob)]
     with engine.Server(p, SERVED_BUDGET, 20000) as srv:
         ids = {}
         nxt = 0
+        late = []
         t0 = time.perf_counter()
         while len(lat) < njob:
             now = time.perf_counter() - t0
-            if now > 900.0:
-                raise RuntimeError("served stream did not drain in 900 s")
+            if now > 1200.0:
+                raise RuntimeError("served stream did not drain in 1200 s")
             while nxt < njob and req["arrival"][nxt] <= now:
-                ids[srv.submit(mols[nxt], xyz[nxt], int(req["steps"][nxt]), float(req["T"][nxt]),
+                m, x = futs[nxt].result()
+                late.append(time.perf_counter() - t0 - req["arrival"][nxt])
+                ids[srv.submit(m, x, int(req["steps"][nxt]), float(req["T"][nxt]),
                                traj=nxt)] = nxt
+                futs[nxt] = None
                 nxt += 1
             s = srv.stats()
             if s["queued"] == 0 and s["active"] == 0 and nxt < njob:
@@ -261,13 +276,14 @@ def served_stream(local: int) -> dict:
                 statuses.append(r["status"])
         wall = time.perf_counter() - t0
         stats = srv.stats()
+    gen.shutdown()
     served_rate = work / wall
-    # the plain path on every 10th job, one context at a time
-    sample = list(range(0, njob, 10))
+    # the plain path on every PLAIN_EVERY-th job, one context at a time
+    sample = list(range(0, njob, PLAIN_EVERY))
     pw, pt = 0, 0.0
     for k in sample:
-        ep = engine.plain(mols[k], xyz[k], p, T=float(req["T"][k]), traj=k,
-                          nsteps=int(req["steps"][k]))
+        m, x = make(k)
+        ep = engine.plain(m, x, p, T=float(req["T"][k]), traj=k, nsteps=int(req["steps"][k]))
         t1 = time.perf_counter()
         ep.step(int(req["steps"][k]))
         pt += time.perf_counter() - t1
@@ -278,15 +294,21 @@ def served_stream(local: int) -> dict:
             "latency_p50_s": float(np.percentile(lv, 50)),
             "latency_p99_s": float(np.percentile(lv, 99)),
             "jobs": njob, "bead_steps": work, "wall_s": wall,
+            "arrival_window_s": SERVED_SECONDS,
+            "submit_lag_p99_s": float(np.percentile(np.array(late), 99)),
+            "offered_bead_steps_per_s": float((req["n"].astype(np.float64) * req["steps"]).sum()
+                                              / SERVED_SECONDS),
             "plain_sequential": pw / pt, "served_over_plain": served_rate / (pw / pt),
+            "plain_sample_jobs": len(sample),
             "failed_jobs": int(sum(1 for s in statuses if s & 3)),
             "device_bytes": stats["device_bytes"],
             "config": f"Poisson {SERVED_RATE:.0f} jobs/s for {SERVED_SECONDS:.0f} s ({njob} jobs), "
                       f"N log-uniform [50,20000], steps log-uniform [{SERVED_STEPS[0]:.0f},"
-                      f"{SERVED_STEPS[1]:.0f}] (the [1e4,1e6] range scaled by 1/50), kBT "
-                      f"U[0.5,0.8], half native / half extended, budget "
-                      f"{SERVED_BUDGET >> 30} GiB, boxl {SERVED_BOXL:.0f} A; plain_sequential: "
-                      f"every 10th job alone, one context at a time"}
+                      f"{SERVED_STEPS[1]:.0f}] (the [1e4,1e6] range scaled by 1/{STEP_SCALE}), "
+                      f"kBT U[0.5,0.8], half native / half extended, HBM budget "
+                      f"{SERVED_BUDGET / 1e9:.0f} GB, boxl {SERVED_BOXL:.0f} A; latency from "
+                      f"submission at the arrival time to retirement; plain_sequential: every "
+                      f"{PLAIN_EVERY}th job ({len(sample)} jobs) alone, one context at a time"}
 
 
 PLAIN = {  # workload: (beads, structure seed, per-contact epsilon range)
@@ -296,24 +318,26 @@ PLAIN = {  # workload: (beads, structure seed, per-contact epsilon range)
 }
 
 
-def plain_one(args, local: int) -> None:
+def plain_measure(workload: str, local: int, K: int, warmup: int, lanes: int = 0, form: int = 0,
+                  cpu_seconds: float = 5.0) -> dict:
     """The plain single-molecule path on one synthetic structure: whole-step
-    rate and each stage's HBM roofline."""
+    rate, each stage's HBM roofline, and the reference algorithm on one host
+    core (cpu_seconds of it; 0 skips it)."""
     import torch
     from sop_gb300 import engine
     dev = torch.device("cuda", local)
     torch.cuda.set_device(local)
-    nbead, seed, eps = PLAIN[args.workload]
+    nbead, seed, eps = PLAIN[workload]
     mol = system.generate(nbead, seed, eps)
-    p = engine.baseline_params(device=local, graph_steps=MD_STEPS, lanes_per_bead=args.lanes,
-                               step_split=args.form)
+    p = engine.baseline_params(device=local, graph_steps=MD_STEPS, lanes_per_bead=lanes,
+                               step_split=form)
     e = engine.plain(mol, mol.xyz, p, T=0.6)
     stream = torch.cuda.ExternalStream(e.stream(), device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         e.step_async(MD_STEPS)
     e.sync()
-    K = args.steps
+    s_start = e.status(0)[1]
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(K)]
     torch.cuda.synchronize(dev)
@@ -363,16 +387,17 @@ def plain_one(args, local: int) -> None:
     tuning = e.tuning()
     e.close()
     s0 = stages[names[0]]
-    n_launch = sum(launches_per_bench_step(p, k * MD_STEPS, tuning["form"]) for k in range(K))
+    n_launch = sum(launches_per_bench_step(p, s_start + k * MD_STEPS, tuning["form"])
+                   for k in range(K))
     cpu = None
-    if not args.no_cpu_baseline:
+    if cpu_seconds > 0:
         # the reference algorithm on one host core, in whole neighbour-list
-        # periods (50 steps, one O(N^2) list build each) until ~5 s have passed
+        # periods (50 steps, one O(N^2) list build each) until cpu_seconds passed
         from oracle import pyoracle as O
         r = O.RefRun(mol, mol.xyz, CUT, 0.05, 0.05, 0.6, 50, 10, 1234, 0)
         r.advance(0)
         done, t_cpu = 0, 0.0
-        while t_cpu < 5.0:
+        while t_cpu < cpu_seconds:
             t0 = time.perf_counter()
             r.advance(50)
             t_cpu += time.perf_counter() - t0
@@ -382,10 +407,10 @@ def plain_one(args, local: int) -> None:
                "sample": f"{done} Langevin steps of this molecule (whole 50-step neighbour-list "
                          f"periods), serial FP32 restatement of the reference's host list filters, "
                          f"force kernels and integrator, one thread"}
-    line = {"metric": f"bead-steps/s (plain path, {nbead:,} beads)", "value": value, "unit": UNIT,
-            "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": 1e3 * t / K,
-            "higher_is_better": True, "scaling": "none", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
+    traffic = profile_traffic(workload)
+    return {"metric": f"bead-steps/s (plain path, {nbead:,} beads)", "value": value, "unit": UNIT,
+            "steps": K, "warmup": warmup, "ms_per_step": 1e3 * t / K,
+            "us_per_md_step": 1e6 * t / (K * MD_STEPS),
             "config": {"workload": f"plain path, one molecule of {nbead:,} beads (seed {seed})"
                                    + (", per-contact epsilon U[0.7,1.3]" if eps else "")
                                    + ", NL 32 A / 50 steps, PL 16 A / 10 steps, "
@@ -393,10 +418,22 @@ def plain_one(args, local: int) -> None:
                        "md_steps_per_bench_step": MD_STEPS,
                        "l2": "flushed before every timed step (256 MiB write)"},
             "roofline": {"bound": "hbm", "achieved": s0["achieved_gbs"], "peak": peak,
-                         "unit": "GB/s", "frac": s0["frac"], "traffic": profile_traffic(args.workload),
+                         "unit": "GB/s", "frac": s0["frac"], "traffic": traffic,
+                         "traffic_source": (f"ncu capture, profiles/step_kernel_{workload}.md"
+                                            if traffic else None),
                          "kernel": names[0], "peak_source": peak_kind},
-            "cpu_baseline": cpu, "tuning": tuning,
-            "stages": stages, "lists": ls, "gpu_launches": int(n_launch), "clocks": clk.summary()}
+            "cpu_baseline": cpu, "tuning": tuning, "stages": stages, "lists": ls,
+            "gpu_launches": int(n_launch), "clocks": clk.summary()}
+
+
+def plain_one(args, local: int) -> None:
+    """`--workload plainN`: the plain path's own JSON line."""
+    d = plain_measure(args.workload, local, args.steps, args.warmup, args.lanes, args.form,
+                      0.0 if args.no_cpu_baseline else 5.0)
+    line = {"metric": d.pop("metric"), "value": d.pop("value"), "unit": d.pop("unit"),
+            "n_gpus": 1, "steps": d.pop("steps"), "warmup": d.pop("warmup"),
+            "ms_per_step": d.pop("ms_per_step"), "higher_is_better": True, "scaling": "none",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", **d}
     print(json.dumps(line), flush=True)
 
 

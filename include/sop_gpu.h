@@ -324,20 +324,26 @@ int sop_serve_resume(void* ctx, const sop_molecule* m, const void* buf, long lon
  * on `stream` (a cudaStream_t, NULL for the default stream) and returns
  * without waiting.
  *
- * Lists are in the reference's layout (energy.cu:194-442), 0-based bead
- * pairs: bonds with native lengths, i,i+2 angle pairs, native pairs with r0
- * and epsilon (NULL: 1.0), non-native pairs.  terms receives 5 doubles as
- * sop_energy: e_bnd, e_ang_ss, e_vdw_rr_att, e_vdw_rr_rep, rna_etot.
+ * Layout: flat arrays of 0-based bead indices, one entry per term -- bonds
+ * (bond_i, bond_j) with their native lengths, i,i+2 angle pairs (ang_i,
+ * ang_k), native pairs (att_i, att_j) with r0 and the epsilon of the native
+ * ENERGY (att_eps; NULL: 1.0 for every pair), non-native pairs (rep_i,
+ * rep_j) -- and a separate per-bead type array (1 or 2, selecting sigma_rep;
+ * NULL: all 1).  Every index must lie in [0, nbead) and every type be 1 or 2:
+ * an entry that breaks this is not evaluated and turns its term and rna_etot
+ * into NaN.  terms receives 5 doubles as sop_energy: e_bnd, e_ang_ss,
+ * e_vdw_rr_att, e_vdw_rr_rep, rna_etot.
  *
  * Limit: at most SOP_ENERGY_NOALLOC_MAX_ITEMS list entries in total (bonds +
  * angles + native + non-native pairs); larger inputs fail with
- * SOP_ERR_CAPACITY.  The per-block partial sums live in one fixed 128 KiB
- * device array that every GPU loading the library holds until the process
- * exits.  The first call on a device looks up that array's device address
- * (cudaGetSymbolAddress) with the device current; make that first call before
- * any stream capture.  Every call shares the array and overwrites the part it
- * uses, so calls that overlap on the GPU (different streams, or different host
- * threads on one device) race; serialise them.
+ * SOP_ERR_CAPACITY before any launch.  The per-block partial sums live in one
+ * fixed 128 KiB device array that every GPU loading the library holds until
+ * the process exits.  Every call looks up that array's device address
+ * (cudaGetSymbolAddress) in the caller's current device and context; the first
+ * call in a context also loads the library's device code there, so make it
+ * before any stream capture.  Every call shares the array and overwrites the
+ * part it uses, so calls that overlap on the GPU (different streams, or
+ * different host threads on one device) race; serialise them.
  */
 #define SOP_ENERGY_NOALLOC_MAX_ITEMS 4194304LL
 typedef struct sop_energy_lists {
@@ -349,7 +355,7 @@ typedef struct sop_energy_lists {
   long long nrep; const int* rep_i; const int* rep_j;
 } sop_energy_lists;
 int sop_energy_noalloc(const sop_params* p, const sop_energy_lists* l, double* terms, void* stream);
-/* Message of the last sop_energy_noalloc failure. */
+/* Message of the calling thread's last sop_energy_noalloc failure. */
 const char* sop_energy_noalloc_error(void);
 
 /* Last error message of the context (or of the library when ctx is NULL). */

@@ -1,5 +1,7 @@
 """ctypes access to the oracle (oracle/liboracle.so) and to the reference's own
-host routines (oracle/_ref/libsopref.so).
+routines (oracle/_ref/libsopref.so: host routines and host list filters;
+oracle/_ref/libsopref_gpu.so: the reference as it ships, list drivers and
+force kernels on a GPU).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
 CPU-baseline leg of bench.py -- never by the engine.
@@ -204,5 +206,58 @@ def ref_lib() -> ctypes.CDLL:
     global _REF
     if _REF is None:
         _REF = ctypes.CDLL(os.path.join(HERE, "_ref", "libsopref.so"))
-        _REF.ref_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+        _bind_ref(_REF)
     return _REF
+
+
+def ref_gpu_available() -> bool:
+    return os.path.exists(os.path.join(HERE, "_ref", "libsopref_gpu.so"))
+
+
+def ref_gpu_lib() -> ctypes.CDLL:
+    """The reference as it ships (GPU list drivers, force kernels); a process
+    loads either this library or ref_lib(), not both."""
+    R = ctypes.CDLL(os.path.join(HERE, "_ref", "libsopref_gpu.so"))
+    _bind_ref(R)
+    return R
+
+
+def _bind_ref(R) -> None:
+    R.ref_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+    R.ref_set.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+    R.ref_device_setup.argtypes = [ctypes.c_ulonglong]
+
+
+def ref_load_molecule(R, mol, x, boxl, prefix) -> None:
+    """Writes mol (coordinates x) in the reference's file formats at prefix and
+    runs the reference's loader on them (io.cpp:112-259) with `set boxl`."""
+    from sop_gb300 import system
+    system.write_reference_files(mol, prefix, x)
+    R.ref_init_defaults()
+    R.ref_set(b"boxl", repr(float(boxl)).encode())
+    for k in ("bonds", "angles", "vdw", "init"):
+        R.ref_load(k.encode(), f"{prefix}.{k}".encode())
+
+
+def ref_lists(R) -> dict:
+    """The reference's list drivers (update_neighbor_list then
+    update_pair_list) on its current coordinates: 0-based (i, j) pairs of the
+    attractive / repulsive neighbour and pair lists, r0 of the attractive ones."""
+    c = np.zeros(4, np.int64)
+    R.ref_update_lists(_p(c))
+    out = {}
+    for w, name in enumerate(("nl_att", "nl_rep", "pl_att", "pl_rep")):
+        k = int(c[w])
+        i = np.zeros(max(k, 1), np.int32)
+        j = np.zeros(max(k, 1), np.int32)
+        r = np.zeros(max(k, 1), np.float32)
+        R.ref_list_copy(w, _p(i), _p(j), _p(r))
+        out[name] = (i[:k].copy(), j[:k].copy(), r[:k].copy())
+    return out
+
+
+def ref_forces(R, n) -> np.ndarray:
+    """force_eval of the reference on its current device pair lists."""
+    f = np.zeros((n, 3), np.float32)
+    R.ref_force_eval(_p(f))
+    return f

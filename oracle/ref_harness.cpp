@@ -1,19 +1,29 @@
-// C-ABI access to the reference's own host routines, for pinning the oracle.
+// C-ABI access to the reference's own routines, for pinning the oracle.
 //
 // TEST INFRASTRUCTURE ONLY.  Linked with the reference's unmodified sources
 // (global.cpp, param.cpp, io.cpp, misc.cpp, random_generator.cpp, energy.cu,
-// sop.cu, GPUvars.cu) into oracle/_ref/libsopref.so by oracle/build_ref.sh.
-// Nothing here touches a GPU: it drives the reference's file loader
-// (io.cpp:112-259), FP32 host energies (energy.cu:194-225, 278-307, 369-442)
-// and observables (sop.cu:528-611) on host arrays.
+// sop.cu, GPUvars.cu) by oracle/build_ref.sh, into
+//   oracle/_ref/libsopref.so      sop.cu with its host list filters; the
+//                                 functions below marked "host" run without a
+//                                 GPU (device arrays stand on host buffers)
+//   oracle/_ref/libsopref_gpu.so  sop.cu as it ships (CUDPP-based GPU list
+//                                 drivers); the "device" functions need a GPU
+// It drives the reference's file loader (io.cpp:112-259), FP32 host energies
+// (energy.cu:194-225, 278-307, 369-442), observables (sop.cu:528-611), its
+// list drivers (sop.cu:924-1262, 1351-1448, 1452-1620, 1707-1823) and its force
+// kernels through force_eval (energy.cu:81-150).
 #include <cstring>
+#include <cstdlib>
 #include "global.h"
 #include "energy.h"
 #include "io.h"
 #include "param.h"
 #include "sop.h"
+#include "GPUvars.h"
 
 extern "C" {
+
+void ref_host_copies(int on);  // oracle/ref_link_wraps.cpp
 
 // Resets the reference's defaults (param.cpp:8-119).
 void ref_init_defaults() { alloc_arrays(); }
@@ -137,6 +147,104 @@ void ref_update_line(double istep, char* out, int cap) {
   rna_etot = e_bnd + e_ang_ss + e_vdw_rr;
   snprintf(out, cap, "%.0lf %f %f %f %f %f %f %f %f %f %d %f", istep, T, kinT, e_bnd, e_ang_ss,
            e_vdw_rr_att, e_vdw_rr_rep, e_vdw_rr, rna_etot, Q, contct_nat, rgsq);
+}
+
+// Runs one `set <key> <value>;` command of the reference's input script
+// (sop.cu:70-73 -> set_params, param.cpp:233-394).
+void ref_set(const char* key, const char* value) {
+  std::strcpy(cmd[1], "set");
+  std::strcpy(opt[1], key);
+  std::strcpy(opt[2], value);
+  opt_ptr[1] = 1;
+  opt_ptr[2] = 3;
+  set_params(1);
+}
+
+// ---- list drivers ---------------------------------------------------------
+
+// host: points the device arrays the host list filters stage through
+// (dev_unc_pos, dev_idx_neighbor_list_*, dev_nl_lj_nat_pdb_dist) at host
+// buffers sized as alloc_GPU_arrays sizes them (GPUvars.cu:105-130), and turns
+// every cudaMemcpy into a host copy.  Call after the loads.
+void ref_host_lists_prepare() {
+  ref_host_copies(1);
+  unc_pos_size = nbead * sizeof(FLOAT3);
+  pos_size = unc_pos_size;
+  vel_size = unc_pos_size;
+  dev_unc_pos = new FLOAT3[nbead];
+  dev_pos = new FLOAT3[nbead];
+  dev_vel = new FLOAT3[nbead];
+  dev_idx_neighbor_list_att = new ushort2[ncon_att > 0 ? ncon_att : 1];
+  dev_nl_lj_nat_pdb_dist = new PDB_FLOAT[ncon_att > 0 ? ncon_att : 1];
+  dev_idx_neighbor_list_rep = new ushort2[ncon_rep > 0 ? ncon_rep : 1];
+  std::memcpy(dev_unc_pos, unc_pos, unc_pos_size);
+}
+
+// device: the reference's device set-up from the loaded globals, as
+// underdamped_ctrl does it (sop.cu:133-140): alloc_GPU_arrays
+// (GPUvars.cu:99-231), alloc_cudpp (GPUvars.cu:232-298), setup_rng
+// (GPUvars.cu:430-453).
+void ref_device_setup(unsigned long long seed) {
+  alloc_GPU_arrays();
+  alloc_cudpp();
+  setup_rng(seed, 0);
+}
+
+// host or device: uploads the host coordinates and velocities to the device
+// arrays (the H2D copies of alloc_GPU_arrays and load_coords).
+void ref_upload_state() {
+  cudaMemcpy(dev_unc_pos, unc_pos, unc_pos_size, cudaMemcpyHostToDevice);
+  cudaMemcpy(dev_pos, pos, pos_size, cudaMemcpyHostToDevice);
+  cudaMemcpy(dev_vel, vel, vel_size, cudaMemcpyHostToDevice);
+}
+
+// host or device: update_neighbor_list followed by update_pair_list, as the
+// set-up of underdamped_ctrl calls them (sop.cu:143-147).  The neighbour list
+// is copied to the host arrays before the pair-list driver reorders the device
+// buffer it shares with the pair list; the pair list after it.  counts
+// receives nnl_att, nnl_rep, nil_att, nil_rep.
+void ref_update_lists(long long* counts) {
+  update_neighbor_list();
+  cudaMemcpy(idx_neighbor_list_att, dev_idx_neighbor_list_att, nnl_att * sizeof(ushort2),
+             cudaMemcpyDeviceToHost);
+  cudaMemcpy(nl_lj_nat_pdb_dist, dev_nl_lj_nat_pdb_dist, nnl_att * sizeof(PDB_FLOAT),
+             cudaMemcpyDeviceToHost);
+  cudaMemcpy(idx_neighbor_list_rep, dev_idx_neighbor_list_rep, nnl_rep * sizeof(ushort2),
+             cudaMemcpyDeviceToHost);
+  update_pair_list();
+  cudaMemcpy(idx_pair_list_att, dev_idx_pair_list_att, nil_att * sizeof(ushort2),
+             cudaMemcpyDeviceToHost);
+  cudaMemcpy(pl_lj_nat_pdb_dist, dev_pl_lj_nat_pdb_dist, nil_att * sizeof(PDB_FLOAT),
+             cudaMemcpyDeviceToHost);
+  cudaMemcpy(idx_pair_list_rep, dev_idx_pair_list_rep, nil_rep * sizeof(ushort2),
+             cudaMemcpyDeviceToHost);
+  counts[0] = nnl_att; counts[1] = nnl_rep; counts[2] = nil_att; counts[3] = nil_rep;
+}
+
+// Copies one list of the last ref_update_lists as 0-based (i, j) pairs in the
+// reference's order, with r0 for the attractive lists (r0 may be NULL).
+// which: 0 attractive NL, 1 repulsive NL, 2 attractive PL, 3 repulsive PL.
+void ref_list_copy(int which, int* i_out, int* j_out, float* r0_out) {
+  const ushort2* src = which == 0 ? idx_neighbor_list_att : which == 1 ? idx_neighbor_list_rep
+                     : which == 2 ? idx_pair_list_att : idx_pair_list_rep;
+  const PDB_FLOAT* r0 = which == 0 ? nl_lj_nat_pdb_dist : which == 2 ? pl_lj_nat_pdb_dist : nullptr;
+  const int n = which == 0 ? nnl_att : which == 1 ? nnl_rep : which == 2 ? nil_att : nil_rep;
+  for (int k = 0; k < n; ++k) {
+    i_out[k] = GET_IDX(src[k].x) - 1;
+    j_out[k] = GET_IDX(src[k].y) - 1;
+    if (r0 && r0_out) r0_out[k] = r0[k];
+  }
+}
+
+// device: force_eval (energy.cu:81-150) -- clear_forces, random_force and the
+// four force kernels -- on the current device pair lists at the current T;
+// the device forces are copied to out (3 floats per bead).
+void ref_force_eval(float* out) {
+  force_eval();
+  cudaMemcpy(force, dev_force, nbead * sizeof(float3), cudaMemcpyDeviceToHost);
+  for (int i = 0; i < nbead; ++i) {
+    out[3 * i] = force[i].x; out[3 * i + 1] = force[i].y; out[3 * i + 2] = force[i].z;
+  }
 }
 
 }  // extern "C"

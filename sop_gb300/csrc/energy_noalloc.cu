@@ -13,13 +13,12 @@
 // in kernels_step.cu), which keeps its per-block partial sums in scratch the
 // context allocates.  Here the scratch is a file-scope __device__ array of
 // fixed size (kMaxBlocks blocks of four doubles, 128 KiB) that every GPU
-// loading this library holds until the process exits.  The lists come in the
-// reference's own layout (pairs of 0-based bead indices, as energy.cu:194-442
-// reads them), one thread per list entry, so no per-bead rows are needed.
+// loading this library holds until the process exits.  The lists are flat
+// arrays of 0-based bead-index pairs with a separate per-bead type array,
+// one thread per list entry, so no per-bead rows are needed.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cmath>
-#include <mutex>
 #include <string>
 
 #include "sop_dev.cuh"
@@ -32,16 +31,14 @@ constexpr int kThreads = 256;
 constexpr int kItemsPerThread = 4;
 constexpr int kMaxBlocks = 4096;
 constexpr long long kMaxItems = (long long)kMaxBlocks * kThreads * kItemsPerThread;
-constexpr int kMaxDevices = 64;
 
 // Partial sums of the four energy terms, one group of four per block.  Each
 // call writes the partials of every block it launches before the final sum
 // reads them, so nothing has to start at zero; concurrent calls share it.
 static __device__ __align__(256) double g_energy_scratch[kMaxBlocks * 4];
 
-std::mutex g_mu;
-double* g_scratch_ptr[kMaxDevices] = {};
-std::string g_err;
+// Message of the calling thread's last failure.
+thread_local std::string g_err;
 
 struct Lists {
   int nbead;
@@ -64,11 +61,17 @@ __device__ __forceinline__ void separation(const float* x, int i, int j, float b
   min_image3(dx, dy, dz, boxl);
 }
 
+__device__ __forceinline__ bool bead_ok(int i, int nbead) { return i >= 0 && i < nbead; }
+
 // One thread per list entry over [bonds | angles | native pairs | non-native
-// pairs]; the same FP32 terms as k_energy, summed in FP64 per block.
+// pairs]; the same FP32 terms as k_energy, summed in FP64 per block.  An
+// entry whose bead index lies outside [0, nbead), or whose bead type is not
+// 1 or 2, is not evaluated: it adds NaN to its term, so the caller sees the
+// bad input in that term and in rna_etot instead of an out-of-bounds read.
 __global__ void __launch_bounds__(kThreads) k_energy_lists(Lists L, double* __restrict__ scratch) {
   __shared__ double red[4][kThreads / 32];
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const double bad = __longlong_as_double(0x7ff8000000000000LL);  // quiet NaN
   const long long n1 = L.nbnd, n2 = n1 + L.nang, n3 = n2 + L.natt, n4 = n3 + L.nrep;
   const long long base = ((long long)blockIdx.x * kThreads + threadIdx.x) * kItemsPerThread;
   for (int q = 0; q < kItemsPerThread; ++q) {
@@ -77,6 +80,7 @@ __global__ void __launch_bounds__(kThreads) k_energy_lists(Lists L, double* __re
     float dx, dy, dz, lx, ly, lz;
     if (e < n1) {
       const int k = (int)e;
+      if (!bead_ok(L.bi[k], L.nbead) || !bead_ok(L.bj[k], L.nbead)) { acc[0] += bad; continue; }
       separation(L.x, L.bi[k], L.bj[k], L.boxl, dx, dy, dz, lx, ly, lz);
       const float r0 = L.br0[k];
       const float r = sqrtf(dx * dx + dy * dy + dz * dz);
@@ -84,11 +88,13 @@ __global__ void __launch_bounds__(kThreads) k_energy_lists(Lists L, double* __re
       acc[0] += (double)log1pf(-dev * dev / L.R0sq);
     } else if (e < n2) {
       const int k = (int)(e - n1);
+      if (!bead_ok(L.ai[k], L.nbead) || !bead_ok(L.ak[k], L.nbead)) { acc[1] += bad; continue; }
       separation(L.x, L.ai[k], L.ak[k], L.boxl, dx, dy, dz, lx, ly, lz);
       const float inv = 1.0f / (dx * dx + dy * dy + dz * dz);
       acc[1] += (double)(L.e_ss * inv * inv * inv);
     } else if (e < n3) {
       const int k = (int)(e - n2);
+      if (!bead_ok(L.pi[k], L.nbead) || !bead_ok(L.pj[k], L.nbead)) { acc[2] += bad; continue; }
       separation(L.x, L.pi[k], L.pj[k], L.boxl, dx, dy, dz, lx, ly, lz);
       const float r0 = L.pr0[k];
       const float d2 = dx * dx + dy * dy + dz * dz;
@@ -100,8 +106,10 @@ __global__ void __launch_bounds__(kThreads) k_energy_lists(Lists L, double* __re
     } else {
       const long long k = e - n3;
       const int i = L.ri[k], j = L.rj[k];
-      separation(L.x, i, j, L.boxl, dx, dy, dz, lx, ly, lz);
+      if (!bead_ok(i, L.nbead) || !bead_ok(j, L.nbead)) { acc[3] += bad; continue; }
       const int ti = L.types ? L.types[i] : 1, tj = L.types ? L.types[j] : 1;
+      if (ti < 1 || ti > 2 || tj < 1 || tj > 2) { acc[3] += bad; continue; }
+      separation(L.x, i, j, L.boxl, dx, dy, dz, lx, ly, lz);
       const float u = pick_type_pair(L.sig2[1][1], L.sig2[1][2], L.sig2[2][2], ti, tj) /
                       (dx * dx + dy * dy + dz * dz);
       const float u3 = u * u * u;
@@ -140,21 +148,17 @@ __global__ void k_energy_lists_final(const double* __restrict__ scratch, int nbl
   if (threadIdx.x == 0) out[4] = t[0] + t[1] + t[2] + t[3];
 }
 
-// Device address of the scratch array on the current device, looked up once
-// per device (the symbol's host-side name is not a device address).
-cudaError_t scratch_for_current_device(double** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+// Device address of the scratch array in the current device's current
+// context.  The symbol's host-side name is not a device address, and the
+// address belongs to a context (a context the caller made itself, or the
+// primary context again after cudaDeviceReset, loads the array elsewhere), so
+// it is looked up on every call rather than cached; the lookup is a host-side
+// table read once the library's device code is loaded in that context.
+cudaError_t scratch_for_current_context(double** out) {
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_energy_scratch);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_energy_scratch);
-    if (e != cudaSuccess) return e;
-    g_scratch_ptr[dev] = static_cast<double*>(p);
-  }
-  *out = g_scratch_ptr[dev];
+  *out = static_cast<double*>(p);
   return cudaSuccess;
 }
 
@@ -187,7 +191,7 @@ int sop_energy_noalloc(const sop_params* p, const sop_energy_lists* l, double* t
     return SOP_ERR_CAPACITY;
   }
   double* scratch = nullptr;
-  cudaError_t e = scratch_for_current_device(&scratch);
+  cudaError_t e = scratch_for_current_context(&scratch);
   if (e != cudaSuccess) {
     g_err = std::string("sop_energy_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e);
     return SOP_ERR_CUDA;

@@ -11,12 +11,24 @@ Fixtures:
   m128_energy.npz              perturbed 128-bead coordinates (seed 0), pair
                                lists, and the reference's FP32 host energies
                                (energy.cu:194-225, 278-307, 369-442) and
-                               observables (sop.cu:528-611) on them, for the
-                               factor-mode and absolute-mode lists
+                               observables (sop.cu:528-611) on them.  The
+                               factor-mode lists are the reference's own: its
+                               host filters update_neighbor_list and
+                               update_pair_list (sop.cu:1351-1448, 1707-1823).
+                               The reference has no absolute cut-off mode; the
+                               absolute-mode (32 / 16 A) lists come from the
+                               oracle and serve only as a larger input to the
+                               reference's energy routines
   m128_out.{traj,traj_unc,coord,unccoord,vel}
                                the reference's output writers (io.cpp:261-381)
                                on that state (wrapped = unwrapped coordinates)
   m128_update.txt              its progress line for step 1000 (sop.cu:256-259)
+  ref_lists.npz                the reference's host-filter neighbour and pair
+                               lists (factor mode, sop.cu:1351-1448, 1707-1823)
+                               for every structure of cases.py: sorted pair
+                               keys for the 128-bead cases, SHA-256 digests of
+                               the sorted keys and the counts for the
+                               4,000-bead ones
 
 Run from the repository root: python tests/golden/make_golden.py
 """
@@ -32,6 +44,9 @@ sys.path.insert(0, ROOT)
 
 from oracle import pyoracle as O  # noqa: E402
 from sop_gb300 import system  # noqa: E402
+
+sys.path.insert(0, HERE)
+import cases  # noqa: E402
 
 
 def P(a):
@@ -82,12 +97,23 @@ def main():
     v = rng.normal(0.0, 0.8, m.xyz.shape).astype(np.float32)
     R.ref_set_state(P(x), P(v))
     fx = {}
+    # factor mode: the reference's own host filters on these coordinates
+    R.ref_set_state(P(x), P(v))
+    R.ref_host_lists_prepare()
+    ref = O.ref_lists(R)
+    nat_key = {(int(a), int(b)): k for k, (a, b) in enumerate(zip(m.nat_i, m.nat_j))}
+    ref_patt = np.array([nat_key[(min(a, b), max(a, b))] for a, b in
+                         zip(*ref["pl_att"][:2])], np.int32)
     for mode, (nlf, nla, plf, pla) in {"factor": (3.2, 0.0, 2.5, 0.0),
                                        "absolute": (0.0, 32.0, 0.0, 16.0)}.items():
-        att = O.filter_att(m, x, None, nlf, nla)
-        ri, rj = O.nl_rep(m, x, nlf, nla)
-        patt = O.filter_att(m, x, att, plf, pla)
-        pri, prj = O.filter_rep(m, x, ri, rj, plf, pla)
+        if mode == "factor":
+            patt = ref_patt
+            pri, prj = ref["pl_rep"][0], ref["pl_rep"][1]
+        else:
+            att = O.filter_att(m, x, None, nlf, nla)
+            ri, rj = O.nl_rep(m, x, nlf, nla)
+            patt = O.filter_att(m, x, att, plf, pla)
+            pri, prj = O.filter_rep(m, x, ri, rj, plf, pla)
         ai = np.ascontiguousarray(m.nat_i[patt]).astype(np.int32)
         aj = np.ascontiguousarray(m.nat_j[patt]).astype(np.int32)
         ar = np.ascontiguousarray(m.nat_r0[patt]).astype(np.float32)
@@ -114,7 +140,29 @@ def main():
         f.write(line.value.decode() + "\n")
     np.savez_compressed(os.path.join(HERE, "m128_energy.npz"), x=x, v=v, observables=ob,
                         coeff_att_11=np.float32(0.7), **fx)
+    reference_case_lists(R)
     print("golden fixtures written to", HERE)
+
+
+def reference_case_lists(R):
+    """ref_lists.npz: the reference's host filters on every case."""
+    import tempfile
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        for name in cases.CASES:
+            mol, x, _, boxl = cases.build(name)
+            O.ref_load_molecule(R, mol, x, boxl, os.path.join(d, name))
+            R.ref_host_lists_prepare()
+            lists = O.ref_lists(R)
+            for which, (i, j, _) in lists.items():
+                keys = cases.pair_keys(mol.n, i, j)
+                out[f"{name}.{which}.count"] = np.int64(len(keys))
+                if name in cases.SMALL:
+                    out[f"{name}.{which}"] = keys
+                else:
+                    out[f"{name}.{which}.sha256"] = np.array(cases.digest(keys))
+            print(name, {k: len(v[0]) for k, v in lists.items()})
+    np.savez_compressed(os.path.join(HERE, "ref_lists.npz"), **out)
 
 
 if __name__ == "__main__":

@@ -129,16 +129,26 @@ def test_rcut_matches_reference_rounding():
     assert O.lib().orc_rcut2(0.0, 32.0, r0) == np.float32(1024.0)
 
 
-def test_reference_shim_compiles_against_reference_headers():
-    """The reference-side shim (the reference's device-side entry points over
-    the C ABI) compiles against the reference's own headers, where a
-    reference tree is present."""
-    import shutil
+def test_dropin_program_links_and_reaches_the_engine(tmp_path):
+    """Where build() found a reference tree, it linked the reference program
+    over the engine (sop_gb300/shim/build_shim_ref.sh).  Run here, without a
+    GPU, the reference's own parser and loaders read an input script and the
+    first replaced call, alloc_GPU_arrays, reaches the engine's C ABI, whose
+    refusal to create a context without a device the shim reports."""
     import subprocess
-    if shutil.which("nvcc") is None:
-        pytest.skip("nvcc not available")
-    script = os.path.join(ROOT, "sop_gb300", "shim", "check_shim.sh")
-    r = subprocess.run(["bash", script], capture_output=True, text=True)
-    if r.returncode == 3:
-        pytest.skip("no reference source tree here")
-    assert r.returncode == 0, r.stderr
+    exe = os.path.join(ROOT, "sop_gb300", "shim", "_build", "sop2_gb300.x")
+    if not os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libsopref.so")):
+        pytest.skip("no reference tree was present at build time")
+    assert os.path.exists(exe), "build() built oracle/_ref but not the drop-in program"
+    from sop_gb300 import system
+    mol = system.generate(32, 1)
+    system.write_reference_files(mol, str(tmp_path / "m"))
+    (tmp_path / "input").write_text(
+        "set dynamics underdamped;\nset temp 0.6;\nset nstep 10;\nset nup 5;\n"
+        "set cutofftype neighborlist;\n" +
+        "".join(f"load {k} {tmp_path / 'm'}.{k};\n" for k in ("bonds", "angles", "vdw", "init")) +
+        "run;\n")
+    r = subprocess.run([exe, "input"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
+    assert "[Finished reading initial coordinates (32)]" in r.stdout
+    if r.returncode != 0:   # no device here: the engine refuses the context
+        assert "sop_ctx_create failed" in r.stderr, r.stderr

@@ -1,15 +1,27 @@
 """The oracle, the file readers and the generator pinned against fixtures made
-by the reference's own host routines (tests/golden/make_golden.py)."""
+by the reference's own routines: its host routines and host list filters
+(tests/golden/make_golden.py, ref_lists.npz) and the reference as it ships,
+run on a GPU (tests/golden/make_ref_gpu.py, ref_gpu.npz: its CUDPP-based list
+drivers and its force kernels)."""
 import os
+import sys
 import tempfile
 
 import numpy as np
 import pytest
 
+from helpers import force_error
 from oracle import pyoracle as O
 from sop_gb300 import system
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+sys.path.insert(0, GOLD)
+import cases  # noqa: E402
+
+# The reference's force kernels are FP32 with float atomics (energy.cu:228-584):
+# against FP64 on the same pair list their error, in the metric of
+# helpers.force_error, stays below this on every case of cases.py.
+REF_FORCE_TOL = 2e-5
 
 
 def _files(prefix):
@@ -61,7 +73,9 @@ def test_oracle_energies_match_reference(mode):
     np.testing.assert_allclose(e, g[f"{mode}_energy"], rtol=2e-5, atol=1e-5)
 
 
-def test_oracle_lists_reproduce_fixture_lists():
+def test_oracle_lists_reproduce_reference_lists():
+    """m128_energy.npz holds the reference's host-filter pair lists
+    (sop.cu:1351-1448, 1707-1823) in the reference's order."""
     g = np.load(os.path.join(GOLD, "m128_energy.npz"))
     m = system.generate(128, 0)
     x = g["x"]
@@ -71,6 +85,74 @@ def test_oracle_lists_reproduce_fixture_lists():
     pi, pj = O.filter_rep(m, x, ri, rj, 2.5, 0.0)
     np.testing.assert_array_equal(pi, g["factor_rep_i"])
     np.testing.assert_array_equal(pj, g["factor_rep_j"])
+
+
+def oracle_case_lists(name):
+    """The oracle's factor-mode lists (3.2 / 2.5) on a case, as sorted keys."""
+    mol, x, _, boxl = cases.build(name)
+    nl_att = O.filter_att(mol, x, None, 3.2, 0.0, boxl)
+    nri, nrj = O.nl_rep(mol, x, 3.2, 0.0, boxl)
+    pl_att = O.filter_att(mol, x, nl_att, 2.5, 0.0, boxl)
+    pri, prj = O.filter_rep(mol, x, nri, nrj, 2.5, 0.0, boxl)
+    k = lambda i, j: cases.pair_keys(mol.n, i, j)  # noqa: E731
+    return {"nl_att": k(mol.nat_i[nl_att], mol.nat_j[nl_att]), "nl_rep": k(nri, nrj),
+            "pl_att": k(mol.nat_i[pl_att], mol.nat_j[pl_att]), "pl_rep": k(pri, prj)}
+
+
+def assert_lists_equal(fx, name, lists):
+    for which, keys in lists.items():
+        assert int(fx[f"{name}.{which}.count"]) == len(keys), (name, which)
+        if name in cases.SMALL:
+            np.testing.assert_array_equal(keys, fx[f"{name}.{which}"], err_msg=f"{name} {which}")
+        else:
+            assert cases.digest(keys) == str(fx[f"{name}.{which}.sha256"]), (name, which)
+
+
+@pytest.mark.parametrize("name", list(cases.CASES))
+def test_oracle_lists_match_reference_host_filters(name):
+    """Bit-exact as sets with the reference's own host filters: native,
+    perturbed and extended starts, two bead types, 128 and 4,000 beads."""
+    fx = np.load(os.path.join(GOLD, "ref_lists.npz"))
+    assert_lists_equal(fx, name, oracle_case_lists(name))
+
+
+def _ref_gpu():
+    path = os.path.join(GOLD, "ref_gpu.npz")
+    if not os.path.exists(path):
+        pytest.skip("ref_gpu.npz not generated")
+    return np.load(path)
+
+
+@pytest.mark.parametrize("name", list(cases.CASES))
+def test_reference_gpu_drivers_match_its_host_filters(name):
+    """The reference as it ships builds its lists with CUDPP sorts on the GPU
+    (sop.cu:924-1262, 1452-1620); on every case they are the sets its host
+    filters give."""
+    g = _ref_gpu()
+    h = np.load(os.path.join(GOLD, "ref_lists.npz"))
+    for which in ("nl_att", "nl_rep", "pl_att", "pl_rep"):
+        assert int(g[f"{name}.{which}.count"]) == int(h[f"{name}.{which}.count"])
+        if name in cases.SMALL:
+            np.testing.assert_array_equal(g[f"{name}.{which}"], h[f"{name}.{which}"])
+        else:
+            assert str(g[f"{name}.{which}.sha256"]) == str(h[f"{name}.{which}.sha256"])
+
+
+@pytest.mark.parametrize("name", [k for k, c in cases.CASES.items() if c["start"] != "extended"])
+def test_oracle_forces_match_reference_kernels(name):
+    """The oracle's FP64 force restatement against the reference's own force
+    kernels (force_eval at T = 0, energy.cu:81-150, 228-584) on the same pair
+    lists: they differ by the reference's FP32 rounding only."""
+    g = _ref_gpu()
+    mol, x, _, boxl = cases.build(name)
+    nl_att = O.filter_att(mol, x, None, 3.2, 0.0, boxl)
+    nri, nrj = O.nl_rep(mol, x, 3.2, 0.0, boxl)
+    pl_att = O.filter_att(mol, x, nl_att, 2.5, 0.0, boxl)
+    pri, prj = O.filter_rep(mol, x, nri, nrj, 2.5, 0.0, boxl)
+    f64, _ = O.forces_f64(mol, x, pl_att, pri, prj, params={"boxl": boxl})
+    err = force_error(g[f"{name}.force"], f64)
+    print(name, "reference kernels vs FP64:", err)
+    assert err <= REF_FORCE_TOL, (name, err)
 
 
 def test_oracle_observables_match_reference():
