@@ -17,9 +17,23 @@ the max over ranks.  Under torchrun each rank runs its own 512-trajectory
 ensemble (replicas: trajectories are independent, no collective), so the
 scaling is weak.
 
+Beside the headline the line carries:
+  roofline      the step kernel timed alone (algorithmic bytes / CUDA-event
+                time); traffic is a profile figure from the committed ncu capture
+  e2e           a 300-step job through the C ABI from host arrays, coordinates
+                copied out every step; set-up time and the steady rate apart
+  cpu_baseline  the reference algorithm on all host cores, bounded sample
+  plain         the plain single-molecule path on the 128-, 4,000- and
+                50,000-bead structures: rate, each stage's roofline, one-core
+                CPU baseline
+  plain_loop    the plain path looping over every 8th ensemble molecule
+  served        the served request stream (Poisson 200 jobs/s for 60 s, 150 GB
+                budget, steps scaled by 1/50), p50 / p99 latency
+
 `--impl reference` times the reference's algorithm on the host cores (the
 serial FP32 CPU restatement of its host routines and kernels, all threads,
-one molecule per thread) on a bounded sample of the same workload.
+one trajectory per task): K steps of all 512 trajectories, and more until
+5 s have passed.
 """
 from __future__ import annotations
 
@@ -45,6 +59,7 @@ METRIC = "aggregate bead-steps/s (batched ensemble)"
 UNIT = "bead-steps/s"
 N_TRAJ = 512
 MD_STEPS = 10
+E2E_STEPS = 300      # bench steps of the end-to-end job (3,000 Langevin steps)
 CUT = [0.0, 32.0, 0.0, 32.0, 0.0, 16.0, 0.0, 16.0]   # absolute NL / PL cut-offs (A)
 
 
@@ -160,18 +175,27 @@ def whole_job_rate(beads_per_rank: int, md_steps: int, world: int, t_max: float)
     return world * beads_per_rank * md_steps / t_max
 
 
-def launches_per_bench_step(p, s0: int, step_kernels: int = 1) -> int:
-    """Kernels of the engine in one replay starting after step s0
-    (step_kernels: 1 for the one-kernel step, 2 for force + finish)."""
+def launches_per_bench_step(p, s0: int, form: int = 1) -> int:
+    """Kernels of the engine in one replay starting after step s0 (form 1:
+    one step kernel per step; 2: force + finish kernels; 3: one persistent
+    launch per run of steps between list rebuilds)."""
     nl_kernels = 12    # bbox reset, bbox, grid, grid base, assign, 3 scan, scatter, cellsort,
                        # stage_xs, nl
     n = 0
+    runs = 0
+    in_run = False
     for k in range(MD_STEPS):
         st = s0 + 1 + k
         nl = p.nnlup > 0 and st % p.nnlup == 0
         pl = nl or p.nplup <= 1 or st % p.nplup == 0
-        n += (nl_kernels if nl else 0) + (1 if pl else 0) + step_kernels
-    return n + 1   # step advance
+        n += (nl_kernels if nl else 0) + (1 if pl else 0)
+        if form == 3:
+            if pl or not in_run:
+                runs += 1
+            in_run = True
+        else:
+            n += 2 if form == 2 else 1
+    return n + runs + 1   # step advance
 
 
 def step_kernel_bytes(e, mols) -> tuple[float, dict]:
@@ -319,7 +343,7 @@ PLAIN = {  # workload: (beads, structure seed, per-contact epsilon range)
 
 
 def plain_measure(workload: str, local: int, K: int, warmup: int, lanes: int = 0, form: int = 0,
-                  cpu_seconds: float = 5.0) -> dict:
+                  cpu_seconds: float = 5.0, window: int = 0) -> dict:
     """The plain single-molecule path on one synthetic structure: whole-step
     rate, each stage's HBM roofline, and the reference algorithm on one host
     core (cpu_seconds of it; 0 skips it)."""
@@ -330,7 +354,7 @@ def plain_measure(workload: str, local: int, K: int, warmup: int, lanes: int = 0
     nbead, seed, eps = PLAIN[workload]
     mol = system.generate(nbead, seed, eps)
     p = engine.baseline_params(device=local, graph_steps=MD_STEPS, lanes_per_bead=lanes,
-                               step_split=form)
+                               step_split=form, step_window=window)
     e = engine.plain(mol, mol.xyz, p, T=0.6)
     stream = torch.cuda.ExternalStream(e.stream(), device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -429,7 +453,7 @@ def plain_measure(workload: str, local: int, K: int, warmup: int, lanes: int = 0
 def plain_one(args, local: int) -> None:
     """`--workload plainN`: the plain path's own JSON line."""
     d = plain_measure(args.workload, local, args.steps, args.warmup, args.lanes, args.form,
-                      0.0 if args.no_cpu_baseline else 5.0)
+                      0.0 if args.no_cpu_baseline else 5.0, args.window)
     line = {"metric": d.pop("metric"), "value": d.pop("value"), "unit": d.pop("unit"),
             "n_gpus": 1, "steps": d.pop("steps"), "warmup": d.pop("warmup"),
             "ms_per_step": d.pop("ms_per_step"), "higher_is_better": True, "scaling": "none",
@@ -437,46 +461,50 @@ def plain_one(args, local: int) -> None:
     print(json.dumps(line), flush=True)
 
 
+REF_MIN_SECONDS = 5.0
+
+
 def run_reference(args, rank: int) -> None:
+    """The reference's algorithm on the host cores: each step is the bench
+    step's 10 Langevin steps of all 512 trajectories, one trajectory per task
+    on every host thread.  K steps are timed, and more until REF_MIN_SECONDS
+    have passed; the rate is over every timed step."""
     from oracle import pyoracle as O
     mols, ts = ensemble(0)
     cores = os.cpu_count() or 1
     runs = [O.RefRun(m, m.xyz, CUT, 0.05, 0.05, float(t), 50, 10, 1234, k)
             for k, (m, t) in enumerate(zip(mols, ts))]
-    beads = np.array([m.n for m in mols])
-    # one reference step: the bench step's 10 Langevin steps, on a rotating
-    # sample of 64 of the 512 trajectories
-    sample = 64
-    order = np.arange(len(runs))
+    beads = int(sum(m.n for m in mols))
+    # largest first, one trajectory per task: the pool balances the load
+    big_first = sorted(runs, key=lambda r: -r.n)
     with ThreadPoolExecutor(cores) as ex:
         list(ex.map(lambda r: r.advance(0), runs))
 
-        def one(step_idx):
-            sel = order[(step_idx * sample) % len(runs):][:sample]
-            if len(sel) < sample:
-                sel = np.concatenate([sel, order[:sample - len(sel)]])
-            # largest first, one trajectory per task: the pool balances the load
-            order_k = sorted(sel.tolist(), key=lambda k: -beads[k])
-            list(ex.map(lambda k: runs[k].advance(MD_STEPS), order_k))
-            return int(beads[sel].sum()) * MD_STEPS
+        def one():
+            list(ex.map(lambda r: r.advance(MD_STEPS), big_first))
 
-        for w in range(args.warmup):
-            one(w)
+        for _ in range(args.warmup):
+            one()
         t0 = time.perf_counter()
-        done = 0
-        for k in range(args.steps):
-            done += one(args.warmup + k)
+        steps = 0
+        while steps < args.steps or time.perf_counter() - t0 < REF_MIN_SECONDS:
+            one()
+            steps += 1
         dt = time.perf_counter() - t0
-    val = done / dt
+    for r in runs:
+        r.close()
+    val = beads * MD_STEPS * steps / dt
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": workload_config(int(beads.sum())),
+            "data": "synthetic", "config": workload_config(beads),
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"each step: {MD_STEPS} Langevin steps of {sample} of the "
-                                       f"512 trajectories (rotating), serial FP32 restatement of "
-                                       f"the reference algorithm, one trajectory per thread at a "
-                                       f"time, {cores} threads"},
+                             "sample": f"{steps} timed steps ({args.steps} asked, more until "
+                                       f"{REF_MIN_SECONDS:.0f} s passed; {dt:.1f} s), each "
+                                       f"{MD_STEPS} Langevin steps of all 512 trajectories "
+                                       f"({beads} beads), serial FP32 restatement of the "
+                                       f"reference algorithm, one trajectory per task on "
+                                       f"{cores} threads"},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -495,7 +523,10 @@ def main() -> None:
     ap.add_argument("--lanes", type=int, default=0,
                     help="lanes per bead of the step kernel (2, 4, 8, 16); 0: autotuned")
     ap.add_argument("--form", type=int, default=0,
-                    help="form of the step: 1 one kernel, 2 force + finish kernels; 0: autotuned")
+                    help="form of the step: 1 one kernel, 2 force + finish kernels, 3 persistent "
+                         "(the steps between rebuilds in one launch); 0: autotuned")
+    ap.add_argument("--window", type=int, default=0,
+                    help="shared-memory window of the step in beads; 0: autotuned, -1: none")
     ap.add_argument("--workload", default="ensemble", choices=["ensemble", *PLAIN],
                     help="ensemble: the batched ensemble (with the served stream beside it); "
                          "plain128 / plain4000 / plain50k: the plain path on one structure")
@@ -533,7 +564,7 @@ def main() -> None:
     mols, ts = ensemble(rank)
     total = sum(m.n for m in mols)
     p = engine.baseline_params(device=local, graph_steps=MD_STEPS, lanes_per_bead=args.lanes,
-                               step_split=args.form)
+                               step_split=args.form, step_window=args.window)
     e = engine.Engine(p)
     for k, (m, t) in enumerate(zip(mols, ts)):
         e.add(m, m.xyz, T=float(t), traj=rank * N_TRAJ + k)
@@ -592,7 +623,7 @@ def main() -> None:
     # ---- end to end through the C ABI: host arrays in, coordinates out every step
     e2e = None
     if not args.no_e2e:
-        K2 = max(10, min(K, 500))
+        K2 = E2E_STEPS
         pinned = [torch.empty((total, 3), dtype=torch.float32, pin_memory=True).numpy()
                   for _ in range(2)]
         h2d = 0
@@ -604,6 +635,7 @@ def main() -> None:
         for k, (m, t) in enumerate(zip(mols, ts)):
             e2.add(m, m.xyz, T=float(t), traj=rank * N_TRAJ + k)
         e2.commit()
+        t_setup = time.perf_counter() - t0
         # each step's coordinates are copied out while the next step runs:
         # queue step k and its download, then wait for download k-1
         prev = None
@@ -619,12 +651,16 @@ def main() -> None:
         e2.close()
         barrier()
         dt = max_over_ranks(dt, world, dev)
+        t_setup = max_over_ranks(t_setup, world, dev)
         e2e = {"value": whole_job_rate(total, MD_STEPS * K2, world, dt), "unit": UNIT,
                "h2d_bytes_per_step": int(h2d / K2), "d2h_bytes_per_step": int(12 * total),
-               "steps": K2, "note": "wall clock: context creation, upload of every structure from "
-                                     "host arrays, set-up, then per step 10 Langevin steps and a "
-                                     "download of every coordinate (sop_download_all_async into "
-                                     "page-locked memory, waited for one step later)"}
+               "steps": K2, "setup_s": t_setup,
+               "steady_value": whole_job_rate(total, MD_STEPS * K2, world, dt - t_setup),
+               "note": f"wall clock of a {K2}-step job through the C ABI: context creation, "
+                       "upload of every structure from host arrays and set-up (setup_s), then "
+                       "per step 10 Langevin steps and a download of every coordinate "
+                       "(sop_download_all_async into page-locked memory, waited for one step "
+                       "later); value includes the set-up, steady_value excludes it"}
 
     cpu = None
     plain = None
@@ -650,6 +686,12 @@ def main() -> None:
                  "sample": f"{len(sample)} of the trajectories (every 8th), {nst} steps each, "
                            f"one plain context at a time (the reference's single-molecule loop)"}
 
+    plains = None
+    if rank == 0 and not args.no_plain:
+        plains = {w: plain_measure(w, local, max(K, 20), args.warmup,
+                                   cpu_seconds=0.0 if args.no_cpu_baseline else 3.0)
+                  for w in PLAIN}
+
     served = None
     if rank == 0 and not args.no_served:
         served = served_stream(local)
@@ -664,6 +706,8 @@ def main() -> None:
             "config": workload_config(total),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
+                         "traffic_source": ("ncu capture of this kernel on this workload, "
+                                            "profiles/step_kernel_ensemble.md" if traffic else None),
                          "kernel": "force + Langevin step (k_step; + k_finish in the two-kernel "
                                    "form)", "step_form": tuning.get("form"),
                          "bytes_per_launch": byts, "launch_us": t_kernel * 1e6,
@@ -675,6 +719,7 @@ def main() -> None:
             "plain_loop": plain,
             "batched_over_plain": (value / world / plain["value"]) if plain else None,
             "served": served,
+            "plain": plains,
             "lists": ls,
             "tuning": tuning,
             "molecule_errors": int(sum(1 for s in statuses if s & 3)),

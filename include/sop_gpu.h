@@ -14,8 +14,9 @@
  * host threads.
  *
  * Indices are 0-based.  The reference stores 1-based 14-bit bead indices with
- * a 2-bit type (global.h:51-67); the engine keeps untyped 32-bit indices and a
- * per-bead type array, so molecules may exceed the reference's 16,383 beads.
+ * a 2-bit type (global.h:51-67); the engine keeps untyped indices and a
+ * per-bead type array: a molecule holds up to 65,535 beads (the reference,
+ * 16,383), a context any number of molecules.
  */
 #ifndef SOP_GPU_H
 #define SOP_GPU_H
@@ -81,8 +82,16 @@ typedef struct sop_params {
                          x += (h / zeta) f with f = F + noise (sop.cu:487-521,
                          a5 = h / zeta, param.cpp:110); velocities stay zero */
   int step_split;     /* form of the step: 1 one kernel, 2 a force kernel and a
-                         finish kernel, 0 chosen by timing at commit (served
+                         finish kernel, 3 every step between two list rebuilds
+                         in one cooperative launch (a device-wide barrier
+                         between steps), 0 chosen by timing at commit (served
                          contexts: 2).  Every form gives the same bits. */
+  int step_window;    /* shared-memory window of the step, in beads: each step
+                         block stages the coordinates of its beads' molecules
+                         (up to this many beads) and gathers partners from
+                         there.  0 chosen by timing at commit, < 0 none, at
+                         most 12288.  Served contexts use none.  Every window
+                         gives the same bits. */
 } sop_params;
 
 /* Fills *p with the reference's defaults and the factor-mode list cut-offs. */
@@ -249,8 +258,24 @@ int sop_memory(void* ctx, int mol, long long* ctx_bytes, long long* mol_bytes);
  * bit-identical for every choice. */
 int sop_tuning(void* ctx, int* lanes, float* ms);
 /* The step's shape in use: lanes per bead, and its form (1 one kernel, 2 a
- * force kernel and a finish kernel). */
+ * force kernel and a finish kernel, 3 persistent: the steps between two list
+ * rebuilds in one launch). */
 int sop_step_form(void* ctx, int* lanes, int* form);
+
+/* The step's shared-memory window in beads (0: partners gathered from global
+ * memory). */
+int sop_step_window(void* ctx, int* wcap);
+
+/*
+ * Health check of the persistent step form's device-wide barrier (no
+ * counterpart in the reference).  Runs three barriers over the persistent
+ * form's grid, with `missing` arrivals that never come (0: the barriers must
+ * complete), each wait limited to timeout_s seconds (at most 10).
+ * *timed_out receives 1 when a wait ran out: the kernel then returns instead
+ * of spinning, the context stays usable and the flag is cleared.  A timed-out
+ * wait inside a step makes sop_step / sop_sync fail with SOP_ERR_CUDA.
+ */
+int sop_check_step_barrier(void* ctx, int missing, double timeout_s, int* timed_out);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that time or order
  * work around the engine. */
@@ -270,7 +295,7 @@ int sop_stream(void* ctx, void** stream);
  * cadence, and its trajectory is bit-identical to the same job run alone.
  */
 int sop_serve_create(const sop_params* p, long long budget_bytes, long long max_job_beads,
-                     void** ctx);
+                     void** ctx);   /* max_job_beads <= 65,535 */
 /* Queues a job (m->nsteps must be >= 0); *job receives its id. */
 int sop_serve_submit(void* ctx, const sop_molecule* m, int* job);
 /* Runs `rounds` rounds; returns when their work is queued on the device. */

@@ -37,7 +37,13 @@ void launch_rebin(const DevSys& s, const NLScratch& w, cudaStream_t st);
 void launch_scan(const int* in, long long n, int* out, int* block_sums, cudaStream_t st);
 long long scan_block_sums_needed(long long n);
 // kernels_step.cu
-void launch_step(const DevSys& s, int G, bool split, int koff, bool step, cudaStream_t st);
+void launch_step(const DevSys& s, int G, bool split, int koff, bool step, int wcap,
+                 cudaStream_t st);
+cudaError_t allow_step_window(int wcap);
+cudaError_t launch_step_persist(const DevSys& s, int G, int koff0, int count, bool step,
+                                unsigned* bar, unsigned long long limit_ns, cudaStream_t st);
+cudaError_t launch_barrier_check(const DevSys& s, int G, unsigned* bar, int missing, int rounds,
+                                 unsigned long long limit_ns, cudaStream_t st);
 void launch_advance(const DevSys& s, int steps, cudaStream_t st);
 void launch_gather_current(const DevSys& s, float* out, int* flag_out, cudaStream_t st);
 void launch_energy(const DevSys& s, int mol_start, int mol_n, int m, double* part, double* out,
@@ -186,6 +192,8 @@ struct SopCtx {
   NLScratch w{};
   int G = 8;
   bool split = false;         // step as force kernel + finish kernel
+  int wcap = 0;               // > 0: step blocks stage their molecules (up to wcap beads)
+  bool persist = false;       // steps between list rebuilds in one cooperative launch
   double* e_part = nullptr;   // energy / observable partials
   double* e_out = nullptr;    // 8 doubles
   double* h_out = nullptr;    // pinned copy of e_out
@@ -291,54 +299,152 @@ int grow_nl_keep(SopCtx* ctx, long long stride);
 
 namespace {
 
+// The rows of beads o .. o + n - 1 of the repulsive neighbour list (r = 0,
+// absolute bead indices) or pair list (r = 1, molecule-relative), every
+// entry as an index relative to bead o, full row stride.
+int read_rows(SopCtx* ctx, int r, int o, int n, std::vector<int>& rows) {
+  const long long stride = ctx->s.nl_stride, len = stride * n;
+  rows.assign((size_t)len, 0);
+  if (!len) return SOP_OK;
+  if (r == 0) {
+    CK(cudaMemcpy(rows.data(), ctx->s.nl_j + (long long)o * stride, sizeof(int) * len,
+                  cudaMemcpyDeviceToHost));
+    for (auto& v : rows) v -= o;
+  } else {
+    std::vector<unsigned short> h((size_t)len);
+    CK(cudaMemcpy(h.data(), ctx->s.pl_j + (long long)o * stride, sizeof(unsigned short) * len,
+                  cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < h.size(); ++k) rows[k] = h[k];
+  }
+  return SOP_OK;
+}
+
 int lanes_for(const SopCtx* ctx) {
   int g = ctx->P.lanes_per_bead;
   if (g == 2 || g == 4 || g == 8 || g == 16) return g;
   return 0;  // autotune
 }
 
-// The step's form: 1 one kernel, 2 force kernel + finish kernel, 0 autotuned.
+// The step's form: 1 one kernel, 2 force kernel + finish kernel, 3 every
+// step between two list rebuilds in one cooperative launch, 0 autotuned.
 int split_for(const SopCtx* ctx) {
   const int f = ctx->P.step_split;
-  return (f == 1 || f == 2) ? f : 0;
+  return (f >= 1 && f <= 3) ? f : 0;
 }
 
-// Picks the lanes per bead G and the form (one kernel or two) of the step for
-// this context by timing the force-only step (idempotent: it recomputes the
-// same forces and look-ahead from the same state) for each candidate not
-// fixed by the parameters; results are bit-identical for every G and form,
-// so only the speed differs.
+// Wait limit of the persistent form's device-wide barrier: a step of the
+// largest context takes well under a millisecond.
+constexpr unsigned long long kBarrierLimitNs = 2000000000ull;
+
+unsigned* barrier_words(SopCtx* ctx) { return reinterpret_cast<unsigned*>(ctx->s.flags + 2); }
+
+// The largest bead window a step block would stage: the bead range from the
+// start of its first bead's molecule to the end of its last bead's, over
+// blocks of `bpb` beads (molecules are contiguous, packed ranges).
+int widest_window(const SopCtx* ctx, int bpb) {
+  std::vector<std::pair<int, int>> r;  // (start, n) by start
+  for (const HostMol& hm : ctx->mols)
+    if (hm.start >= 0 && hm.n > 0) r.emplace_back(hm.start, hm.n);
+  std::sort(r.begin(), r.end());
+  int widest = 0;
+  size_t m0 = 0, m1 = 0;
+  for (long long b0 = 0; b0 < ctx->s.nlive; b0 += bpb) {
+    const long long bl = std::min<long long>(b0 + bpb, ctx->s.nlive) - 1;
+    while (m0 + 1 < r.size() && r[m0 + 1].first <= b0) ++m0;
+    if (m1 < m0) m1 = m0;
+    while (m1 + 1 < r.size() && r[m1 + 1].first <= bl) ++m1;
+    if (m0 < r.size())
+      widest = std::max(widest, r[m1].first + r[m1].second - r[m0].first);
+  }
+  return widest;
+}
+
+// The step's window: sop_params.step_window > 0 fixes it, < 0 turns it off,
+// 0 lets the autotuner choose.
+int window_param(const SopCtx* ctx) { return ctx->P.step_window; }
+constexpr int kMaxStepWindow = 12288;  // 192 KB of shared memory per block
+constexpr int kMaxMolBeads = 65535;    // 16-bit molecule-relative pair-list partners
+
+// Picks the lanes per bead G, the form (one kernel or two) and the shared-
+// memory window of the step for this context by timing the force-only step
+// (idempotent: it recomputes the same forces and look-ahead from the same
+// state) for each candidate not fixed by the parameters; results are
+// bit-identical for every G, form and window, so only the speed differs.
+// Window candidates: none, and 1,024 / 2,048 beads (16 / 32 KB of shared
+// memory per block) where some block's molecules fit.
 int autotune_lanes(SopCtx* ctx) {
-  const int fixed_g = lanes_for(ctx), fixed_f = split_for(ctx);
+  const int fixed_g = lanes_for(ctx), fixed_f = split_for(ctx), fixed_w = window_param(ctx);
   const int cand[4] = {2, 4, 8, 16};
+  std::vector<int> wins = {0};
+  if (!ctx->served && fixed_w > 0) {
+    wins = {fixed_w};
+  } else if (!ctx->served && fixed_w == 0) {
+    // widest window over blocks of 64 beads (the widest blocks, G = 2)
+    const int need = widest_window(ctx, 64);
+    bool small = false;
+    for (const HostMol& hm : ctx->mols) small |= hm.start >= 0 && hm.n > 0 && hm.n <= 2048;
+    if (small) {
+      if (need <= 2048) {
+        wins.push_back((need + 63) / 64 * 64);
+        if (need > 1024) wins.push_back(1024);
+      } else {
+        wins.push_back(1024);
+        wins.push_back(2048);
+      }
+    }
+  }
+  // the opt-in is a per-kernel ceiling shared by every context of the
+  // process: always the same (largest) value, so contexts never lower it
+  // under one another; each launch asks for its own window only
+  if (wins.size() > 1 || wins[0] > 0) CK(allow_step_window(kMaxStepWindow));
   cudaEvent_t a, b;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
   float best = 1e30f;
   int bestg = fixed_g ? fixed_g : 8;
-  bool bests = fixed_f == 2;
+  int bestf = fixed_f ? fixed_f : 1;
+  int bestw = wins[0];
   for (int g : cand) {
     if (fixed_g && g != fixed_g) continue;
     float gbest = 1e30f;
-    for (int f = 1; f <= 2; ++f) {
+    for (int f = 1; f <= 3; ++f) {
       if (fixed_f && f != fixed_f) continue;
+      if (f == 3 && ctx->served) continue;
       const bool sp = f == 2;
-      launch_step(ctx->s, g, sp, 0, false, ctx->stream);  // warm-up
-      CK(cudaEventRecord(a, ctx->stream));
-      for (int r = 0; r < 3; ++r) launch_step(ctx->s, g, sp, 0, false, ctx->stream);
-      CK(cudaEventRecord(b, ctx->stream));
-      CK(cudaEventSynchronize(b));
-      float ms = 0.f;
-      CK(cudaEventElapsedTime(&ms, a, b));
-      gbest = std::min(gbest, ms / 3.0f);
-      if (ms < best) { best = ms; bestg = g; bests = sp; }
+      for (int wc : wins) {
+        if (f == 3 && wc != 0) continue;
+        // three force-only evaluations (idempotent): three launches, or one
+        // persistent launch with barriers between them
+        auto run = [&](int reps) -> cudaError_t {
+          if (f == 3)
+            return launch_step_persist(ctx->s, g, 0, reps, false, barrier_words(ctx),
+                                       kBarrierLimitNs, ctx->stream);
+          for (int r = 0; r < reps; ++r) launch_step(ctx->s, g, sp, 0, false, wc, ctx->stream);
+          return cudaGetLastError();
+        };
+        CK(run(1));  // warm-up
+        CK(cudaEventRecord(a, ctx->stream));
+        CK(run(3));
+        CK(cudaEventRecord(b, ctx->stream));
+        CK(cudaEventSynchronize(b));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, a, b));
+        gbest = std::min(gbest, ms / 3.0f);
+        if (ms < best) { best = ms; bestg = g; bestf = f; bestw = wc; }
+      }
     }
     ctx->tuning[g] = gbest;
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
+  int flags = 0;
+  CK(cudaMemcpy(&flags, ctx->s.flags, sizeof(int), cudaMemcpyDeviceToHost));
+  if (flags & FLAG_BARRIER_TIMEOUT)
+    return ctx->fail(SOP_ERR_CUDA, "the persistent step's barrier timed out while tuning");
   ctx->G = bestg;
-  ctx->split = bests;
+  ctx->split = bestf == 2;
+  ctx->persist = bestf == 3;
+  ctx->wcap = bestw;
   return SOP_OK;
 }
 
@@ -352,7 +458,7 @@ int alloc_nl(SopCtx* ctx, long long stride) {
   ctx->dfree(ctx->s.nl_j);
   ctx->dfree(ctx->s.pl_j);
   ctx->s.nl_j = ctx->dalloc<int>(entries);
-  ctx->s.pl_j = ctx->dalloc<int>(entries);
+  ctx->s.pl_j = ctx->dalloc<unsigned short>(entries);
   if (!ctx->s.nl_j || !ctx->s.pl_j) return ctx->fail(SOP_ERR_ALLOC, "neighbour-list allocation failed");
   ctx->s.nl_stride = stride;
   ctx->drop_graphs();  // kernel arguments changed
@@ -394,7 +500,20 @@ int nl_rebuild_checked(SopCtx* ctx, int koff, int only_mol = -1) {
 }
 
 void force_eval_async(SopCtx* ctx) {
-  launch_step(ctx->s, ctx->G, ctx->split, 0, false, ctx->stream);
+  launch_step(ctx->s, ctx->G, ctx->split, 0, false, ctx->wcap, ctx->stream);
+}
+
+// Step kernels for steps koff0 .. koff0 + count - 1 of a block (no rebuild
+// among them): one persistent launch, or one launch per step.
+void launch_steps(SopCtx* ctx, int koff0, int count) {
+  if (count <= 0) return;
+  if (ctx->persist) {
+    launch_step_persist(ctx->s, ctx->G, koff0, count, true, barrier_words(ctx), kBarrierLimitNs,
+                        ctx->stream);
+    return;
+  }
+  for (int k = koff0; k < koff0 + count; ++k)
+    launch_step(ctx->s, ctx->G, ctx->split, k, true, ctx->wcap, ctx->stream);
 }
 
 // Which rebuilds precede step n (1-based): bit 0 neighbour list, bit 1 pair list.
@@ -408,12 +527,17 @@ int rebuilds_before(const sop_params& P, long long n) {
 // Launch sequence of steps s0+1 .. s0+count (koff 0 .. count-1) and the
 // step-count advance.
 void enqueue_block(SopCtx* ctx, long long s0, int count) {
+  int run0 = 0;  // first step of the current run without rebuilds
   for (int k = 0; k < count; ++k) {
     int r = rebuilds_before(ctx->P, s0 + 1 + k);
+    if (r) {
+      launch_steps(ctx, run0, k - run0);
+      run0 = k;
+    }
     if (r & 1) launch_nl_rebuild(ctx->s, ctx->w, k, ctx->stream);
     if (r & 2) launch_pl_rebuild(ctx->s, k, ctx->stream);
-    launch_step(ctx->s, ctx->G, ctx->split, k, true, ctx->stream);
   }
+  launch_steps(ctx, run0, count - run0);
   launch_advance(ctx->s, count, ctx->stream);
 }
 
@@ -475,11 +599,23 @@ int step_async(SopCtx* ctx, long long nsteps) {
 
 // Waits for queued work; on a neighbour-list overflow regrows the list and
 // re-runs the steps that were skipped.
+// A timed-out wait of the persistent step's barrier leaves the steps it was
+// running half done: the flag and the barrier words are cleared (so the
+// context can be restored from a checkpoint) and the failure reported.
+int barrier_failure(SopCtx* ctx) {
+  CK(cudaMemsetAsync(ctx->s.flags, 0, 4 * sizeof(int), ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return ctx->fail(SOP_ERR_CUDA,
+                   "the persistent step's device-wide barrier timed out; the state of the "
+                   "steps it was running is undefined");
+}
+
 int sync_checked(SopCtx* ctx) {
   for (int round = 0; round < 8; ++round) {
     int flags = 0;
     CK(cudaMemcpyAsync(&flags, ctx->s.flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (flags & FLAG_BARRIER_TIMEOUT) return barrier_failure(ctx);
     if (!(flags & FLAG_NL_OVERFLOW)) return SOP_OK;
     // Every molecule froze at the start of the block that overflowed; the
     // context's clock stopped there too.
@@ -603,7 +739,7 @@ int alloc_pools(SopCtx* ctx, const Caps& c) {
   s.bead_slot = ctx->dalloc<int>(nb);
   s.sorted = ctx->dalloc<int>(nb);
   s.xs = ctx->dalloc<float4>(nb);
-  s.flags = ctx->dalloc<int>(1);
+  s.flags = ctx->dalloc<int>(4);  // [0] flags, [2..3] the persistent step's barrier
   s.noise = nullptr;
   s.use_noise = 0;
   ctx->w.ncell = ctx->dalloc<int>(nm);
@@ -627,7 +763,7 @@ int alloc_pools(SopCtx* ctx, const Caps& c) {
   CK(cudaMemsetAsync(s.mol_step, 0, sizeof(long long) * nm, st));
   CK(cudaMemsetAsync(s.mol_status, 0, sizeof(int) * nm, st));
   CK(cudaMemsetAsync(s.sys_step, 0, sizeof(long long), st));
-  CK(cudaMemsetAsync(s.flags, 0, sizeof(int), st));
+  CK(cudaMemsetAsync(s.flags, 0, 4 * sizeof(int), st));
   CK(cudaMemsetAsync(s.nl_maxrow, 0, sizeof(int), st));
   CK(cudaMemsetAsync(s.nl_att_cnt, 0, sizeof(int) * nb, st));
   CK(cudaMemsetAsync(s.pl_att_cnt, 0, sizeof(int) * nb, st));
@@ -847,9 +983,15 @@ int uninstall(SopCtx* ctx, int slot) {
 // Set-up after installing molecules at step 0: lists from x_0, f_0 and the
 // look-ahead (sop.cu:142-186), and the lanes-per-bead choice.
 int setup_step0(SopCtx* ctx) {
-  const int fixed_g = lanes_for(ctx), fixed_f = split_for(ctx);
+  const int fixed_g = lanes_for(ctx), fixed_f = split_for(ctx), fixed_w = window_param(ctx);
   ctx->G = fixed_g ? fixed_g : 8;
   ctx->split = fixed_f == 2;
+  ctx->persist = fixed_f == 3 && !ctx->served;
+  ctx->wcap = 0;
+  if (fixed_w > 0 && !ctx->served) {
+    CK(allow_step_window(kMaxStepWindow));
+    ctx->wcap = fixed_w;
+  }
   // block offset -1: these rebuilds precede the force evaluation of the
   // current step itself (x_0 sits in both coordinate buffers)
   int rc = nl_rebuild_checked(ctx, -1);
@@ -857,7 +999,7 @@ int setup_step0(SopCtx* ctx) {
   launch_pl_rebuild(ctx->s, -1, ctx->stream);
   force_eval_async(ctx);
   CK(cudaGetLastError());
-  if (!fixed_g || !fixed_f) {
+  if (!fixed_g || !fixed_f || (!fixed_w && !ctx->served)) {
     rc = autotune_lanes(ctx);
     if (rc) return rc;
   }
@@ -970,13 +1112,14 @@ void sop_params_default(sop_params* p) {
   p->seed = 1234;       // setup_rng(1234, 0), sop.cu:138
   p->integrator = 0;    // underdamped (param.cpp:249-253 selects)
   p->step_split = 0;    // autotuned
+  p->step_window = 0;   // autotuned
 }
 
 int sop_ctx_create(const sop_params* p, void** out) {
   if (!p || !out) return SOP_ERR_ARG;
   *out = nullptr;
   if (p->boxl <= 0 || p->h <= 0 || p->R0 <= 0 || p->graph_steps < 0 || p->integrator < 0 ||
-      p->step_split < 0 || p->step_split > 2 ||
+      p->step_split < 0 || p->step_split > 3 || p->step_window > kMaxStepWindow ||
       p->integrator > 1 || (p->integrator == 1 && p->zeta <= 0)) {
     g_lib_error = "invalid parameters";
     return SOP_ERR_ARG;
@@ -1012,6 +1155,9 @@ int sop_ctx_destroy(void* p) {
 // Validates a molecule description and copies it to host storage.
 static int make_hostmol(SopCtx* ctx, const sop_molecule* m, HostMol& h) {
   if (m->nbead <= 0 || !m->unc_pos) return ctx->fail(SOP_ERR_ARG, "molecule needs beads and coordinates");
+  if (m->nbead > kMaxMolBeads)
+    return ctx->fail(SOP_ERR_ARG, "a molecule holds at most 65,535 beads (pair-list rows store "
+                                  "16-bit molecule-relative partners)");
   if (m->nbnd < 0 || m->nang < 0 || m->nnat < 0) return ctx->fail(SOP_ERR_ARG, "negative counts");
   if ((m->nbnd && (!m->bond_i || !m->bond_j || !m->bond_r0)) || (m->nang && (!m->ang_i || !m->ang_k)) ||
       (m->nnat && (!m->nat_i || !m->nat_j || !m->nat_r0)))
@@ -1126,14 +1272,14 @@ int grow_nl_keep(SopCtx* ctx, long long stride) {
   const long long nb = s.nbead, old = s.nl_stride, entries = stride * nb;
   if (entries > (1LL << 40)) return ctx->fail(SOP_ERR_CAPACITY, "neighbour list exceeds 2^40 entries");
   int* nj = ctx->dalloc<int>(entries);
-  int* pj = ctx->dalloc<int>(entries);
+  unsigned short* pj = ctx->dalloc<unsigned short>(entries);
   if (!nj || !pj) {
     ctx->dfree(nj);
     ctx->dfree(pj);
     return ctx->fail(SOP_ERR_ALLOC, "neighbour-list allocation failed");
   }
   CK(cudaMemcpy2D(nj, 4 * stride, s.nl_j, 4 * old, 4 * old, nb, cudaMemcpyDeviceToDevice));
-  CK(cudaMemcpy2D(pj, 4 * stride, s.pl_j, 4 * old, 4 * old, nb, cudaMemcpyDeviceToDevice));
+  CK(cudaMemcpy2D(pj, 2 * stride, s.pl_j, 2 * old, 2 * old, nb, cudaMemcpyDeviceToDevice));
   ctx->dfree(s.nl_j);
   ctx->dfree(s.pl_j);
   s.nl_j = nj;
@@ -1199,13 +1345,13 @@ int checkpoint_of(SopCtx* ctx, int slot, std::vector<char>& out) {
       put(&q, sizeof q);
     }
   const long long stride = s.nl_stride;
-  std::vector<int> rows((size_t)(stride * n));
+  std::vector<int> rows;
   for (int r = 0; r < 2; ++r) {
-    CK(cudaMemcpy(rows.data(), (r == 0 ? s.nl_j : s.pl_j) + (long long)o * stride,
-                  sizeof(int) * rows.size(), cudaMemcpyDeviceToHost));
+    int rc = read_rows(ctx, r, o, n, rows);
+    if (rc) return rc;
     for (int i = 0; i < n; ++i)
       for (int t = 0; t < cnt[(size_t)(2 + r) * n + i]; ++t) {
-        int v = rows[(size_t)i * stride + t] - o;
+        int v = rows[(size_t)i * stride + t];
         put(&v, sizeof v);
       }
   }
@@ -1276,13 +1422,13 @@ int restore_into(SopCtx* ctx, int slot, const char* buf, long long len) {
   const long long stride = s.nl_stride;
   std::vector<int> rows[2];
   for (int k = 0; k < 2; ++k) {
-    rows[k].assign((size_t)(stride * n), o);
+    rows[k].assign((size_t)(stride * n), k == 0 ? o : 0);
     for (int i = 0; i < n; ++i)
       for (int t = 0; t < cnt[(size_t)(2 + k) * n + i]; ++t) {
         int v;
         get(&v, sizeof v);
         if (v < 0 || v >= n) return ctx->fail(SOP_ERR_ARG, "corrupt checkpoint");
-        rows[k][(size_t)i * stride + t] = v + o;
+        rows[k][(size_t)i * stride + t] = k == 0 ? v + o : v;
       }
   }
   const int cur = (int)(h.step & 1);
@@ -1299,7 +1445,8 @@ int restore_into(SopCtx* ctx, int slot, const char* buf, long long len) {
   }
   CK(cudaMemcpy(s.nl_j + (long long)o * stride, rows[0].data(), sizeof(int) * rows[0].size(),
                 cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s.pl_j + (long long)o * stride, rows[1].data(), sizeof(int) * rows[1].size(),
+  std::vector<unsigned short> prow(rows[1].begin(), rows[1].end());
+  CK(cudaMemcpy(s.pl_j + (long long)o * stride, prow.data(), sizeof(unsigned short) * prow.size(),
                 cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s.mol_step + slot, &h.step, sizeof(long long), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s.mol_status + slot, &h.status, sizeof(int), cudaMemcpyHostToDevice));
@@ -1409,7 +1556,8 @@ int sop_add_molecule(void* p, const sop_molecule* m, int* mol_id) {
 
 int sop_serve_create(const sop_params* p, long long budget_bytes, long long max_job_beads,
                      void** out) {
-  if (!p || !out || budget_bytes <= 0 || max_job_beads <= 0) return SOP_ERR_ARG;
+  if (!p || !out || budget_bytes <= 0 || max_job_beads <= 0 || max_job_beads > kMaxMolBeads)
+    return SOP_ERR_ARG;
   if (p->nnlup <= 0) {
     g_lib_error = "serving needs a neighbour-list cadence (nnlup > 0)";
     return SOP_ERR_ARG;
@@ -1458,6 +1606,7 @@ int sop_serve_create(const sop_params* p, long long budget_bytes, long long max_
   const int fixed_g = lanes_for(ctx), fixed_f = split_for(ctx);
   ctx->G = fixed_g ? fixed_g : 4;
   ctx->split = fixed_f != 1;
+  ctx->persist = false;
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->committed = true;
   ctx->host_step = 0;
@@ -1636,7 +1785,7 @@ int sop_launch_stage(void* p, int stage, int koff) {
   SopCtx* ctx = C(p);
   if (!ctx->committed) return ctx->fail(SOP_ERR_ARG, "context not committed");
   switch (stage) {
-    case 0: launch_step(ctx->s, ctx->G, ctx->split, koff, true, ctx->stream); break;
+    case 0: launch_steps(ctx, koff, 1); break;
     case 1: launch_pl_rebuild(ctx->s, koff, ctx->stream); break;
     case 2: launch_nl_rebuild(ctx->s, ctx->w, koff, ctx->stream); break;
     case 3: launch_advance(ctx->s, koff, ctx->stream); break;
@@ -1801,13 +1950,11 @@ int sop_download_list(void* p, int mol, int which, long long cap, int* i_out, in
     CK(cudaMemcpy(cnt.data(), (which == 1 ? ctx->s.nl_cnt : ctx->s.pl_cnt) + o, sizeof(int) * n,
                   cudaMemcpyDeviceToHost));
     const long long stride = ctx->s.nl_stride;
-    size_t len = (size_t)(stride * n);
-    std::vector<int> jj(len);
-    if (len)
-      CK(cudaMemcpy(jj.data(), (which == 1 ? ctx->s.nl_j : ctx->s.pl_j) + stride * o,
-                    sizeof(int) * len, cudaMemcpyDeviceToHost));
+    std::vector<int> jj;
+    int rc = read_rows(ctx, which == 1 ? 0 : 1, o, n, jj);
+    if (rc) return rc;
     for (int i = 0; i < n; ++i)
-      for (int t = 0; t < cnt[i]; ++t) emit(i, jj[(size_t)i * stride + t] - o, 0.f);
+      for (int t = 0; t < cnt[i]; ++t) emit(i, jj[(size_t)i * stride + t], 0.f);
   }
   if (count) *count = k;
   return SOP_OK;
@@ -2080,7 +2227,33 @@ int sop_step_form(void* p, int* lanes, int* form) {
   if (!p) return SOP_ERR_ARG;
   SopCtx* ctx = C(p);
   if (lanes) *lanes = ctx->G;
-  if (form) *form = ctx->split ? 2 : 1;
+  if (form) *form = ctx->persist ? 3 : ctx->split ? 2 : 1;
+  return SOP_OK;
+}
+
+int sop_check_step_barrier(void* p, int missing, double timeout_s, int* timed_out) {
+  if (!p || !timed_out || missing < 0 || !(timeout_s > 0.0) || timeout_s > 10.0)
+    return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (!ctx->committed) return ctx->fail(SOP_ERR_ARG, "context not committed");
+  int rc = sync_checked(ctx);
+  if (rc) return rc;
+  CK(launch_barrier_check(ctx->s, ctx->G, barrier_words(ctx), missing, 3,
+                          (unsigned long long)(timeout_s * 1e9), ctx->stream));
+  int flags = 0;
+  CK(cudaMemcpyAsync(&flags, ctx->s.flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  *timed_out = (flags & FLAG_BARRIER_TIMEOUT) ? 1 : 0;
+  if (*timed_out) {
+    CK(cudaMemsetAsync(ctx->s.flags, 0, 4 * sizeof(int), ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return SOP_OK;
+}
+
+int sop_step_window(void* p, int* wcap) {
+  if (!p || !wcap) return SOP_ERR_ARG;
+  *wcap = C(p)->wcap;
   return SOP_OK;
 }
 

@@ -357,7 +357,8 @@ __device__ __forceinline__ float slab_dist(float v, float a, float w) {
 // d^2 < (fac*sigma or abs)^2 in FP32, |i - j| > 2, not a native contact) are
 // written to the bead's fixed-stride row in candidate order (group ballot).
 // The culling is conservative (a 1e-3 A margin); membership is decided by the
-// exact predicate alone.  The bead's native partners sit in registers.
+// exact predicate alone.  The bead's native partners sit in registers, with
+// a 64-bit filter of their indices in front of the compares.
 template <bool UNI>
 __global__ void __launch_bounds__(256) k_nl(DevSys s) {
   const int k = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) / kNlLanes);
@@ -388,6 +389,13 @@ __global__ void __launch_bounds__(256) k_nl(DevSys s) {
   int nat[kNatRegs];
 #pragma unroll
   for (int q = 0; q < kNatRegs; ++q) nat[q] = q < nrow.y ? s.nat_j[nrow.x + q] : -1;
+  // a 64-bit filter of the native partners (bit j & 63): a candidate whose
+  // bit is clear is no native partner, so most candidates skip the compares
+  unsigned long long nfilter = 0ull;
+#pragma unroll
+  for (int q = 0; q < kNatRegs; ++q)
+    if (nat[q] >= 0) nfilter |= 1ull << (nat[q] & 63);
+  for (int q = kNatRegs; q < nrow.y; ++q) nfilter |= 1ull << (s.nat_j[nrow.x + q] & 63);
   const long long stride = s.nl_stride;
   int* row = s.nl_j + (long long)i * stride;
   int cnt = 0;
@@ -423,7 +431,7 @@ __global__ void __launch_bounds__(256) k_nl(DevSys s) {
                   dz2 = __fsub_rn(xj.z, xi.z);
             if (wrap) min_image3(dx, dy2, dz2, boxl);
             pass = d2_exact(dx, dy2, dz2) < (UNI ? r11 : pick_type_pair(r11, r12, r22, ti, wj & 3));
-            if (pass) {
+            if (pass && ((nfilter >> (j & 63)) & 1ull)) {
               bool native = false;
 #pragma unroll
               for (int q = 0; q < kNatRegs; ++q) native |= (nat[q] == j);
@@ -481,7 +489,8 @@ __global__ void __launch_bounds__(256, 5) k_pl(DevSys s, int koff) {  // 48 regi
   const unsigned lt = (1u << lane) - 1u;
   const long long a = (long long)i * s.nl_stride;
   const int4* row4 = reinterpret_cast<const int4*>(s.nl_j + a);
-  int* out = s.pl_j + a;
+  unsigned short* out = s.pl_j + a;  // partners relative to the molecule's first bead
+  const int mstart = s.mol[m].start;
   const int cnt = s.nl_cnt[i];
   const int2 row = s.nat_row[i];
   const int acnt = s.nl_att_cnt[i];
@@ -517,7 +526,7 @@ __global__ void __launch_bounds__(256, 5) k_pl(DevSys s, int koff) {  // 48 regi
     int pos = k + incl - c;
 #pragma unroll
     for (int q = 0; q < 4; ++q)
-      if (pb & (1u << q)) out[pos++] = jq[q];
+      if (pb & (1u << q)) out[pos++] = (unsigned short)(jq[q] - mstart);
     k += __shfl_sync(gmask, incl, kPlLanes - 1, kPlLanes);
   }
   if (lane == 0) s.pl_cnt[i] = k;

@@ -18,6 +18,8 @@
 // (incr, positions, forces, velocities) regrouped so one kernel per step
 // suffices.  x_n lives in buffer n & 1, so neither the host nor a graph has
 // to track parity, and every molecule may sit at its own step.
+#include <algorithm>
+
 #include "sop_dev.cuh"
 #include "../../include/sop_gpu.h"
 
@@ -96,170 +98,263 @@ constexpr int kOddStep = 4;   // the step is odd: coordinates in buffer 1
 template <bool STEP>
 __device__ __forceinline__ void finish_bead(const DevSys& s, int b, int m, float4 fs, int koff);
 
+// Coordinate sources of the force sum: the molecule's coordinate buffer in
+// global memory, or the block's window of it staged in shared memory (bead j
+// at xw[j - off]).  The arithmetic is the same either way, so are the bits.
+struct GlobalX {
+  const float4* __restrict__ p;
+  __device__ __forceinline__ float4 operator()(int j) const { return p[j]; }
+};
+struct WindowX {
+  const float4* p;  // shared memory
+  int off;
+  __device__ __forceinline__ float4 operator()(int j) const { return p[j - off]; }
+};
+
+// The conservative force on bead i, summed by the G lanes of its group over
+// its rows (bonds, angles, native pair list, repulsive pair list) into the
+// lane's kC virtual-lane accumulators, reduced to lane 0 of the group.
+// Forces are summed in a fixed order whatever G is: entry e of a row
+// accumulates into virtual lane e % kV (in increasing e), and the kV partial
+// sums combine in one fixed binary tree (pairs v, v + kV/2, then v, v + kV/4,
+// ...).  Each physical lane holds kC = kV / G virtual lanes and does the
+// upper tree levels locally, the rest by shuffles.  So every G gives
+// bit-identical forces, and G is free to tune per context.
+template <int G, bool UNI, class XS>
+__device__ __forceinline__ void bead_force(const DevSys& s, const XS& X, int i, int m1, int lane,
+                                           int2 br, int2 ar, int abase, int acnt, int rcnt,
+                                           float& fx, float& fy, float& fz, bool& fene_bad) {
+  constexpr int kC = kV / G;
+  float ax[kC], ay[kC], az[kC];
+#pragma unroll
+  for (int c = 0; c < kC; ++c) ax[c] = ay[c] = az[c] = 0.f;
+  const unsigned gmask = (G == 32) ? 0xffffffffu
+                                   : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+  const float4 xi = X(i);
+  const float boxl = s.boxl;
+  // 0 when no pair of the molecule can reach boxl/4 (from its last binning,
+  // with a cut-off of margin): the minimum image is then the identity and
+  // its test is skipped
+  const bool wrap = s.grid[m1].wrap != 0;
+  const long long rbase = (long long)i * s.nl_stride;
+
+  // Bonded, angle and native terms share one index space [bonds | angles |
+  // natives]; a bead has a handful of them, usually one pass.
+  const int nba = br.y + ar.y;
+  const int nsmall = nba + acnt;
+  for (int base = 0; base < nsmall; base += kV) {
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+      const int e = base + lane + c * G;
+      if (e >= nsmall) continue;
+      int j, t;
+      float r0 = 0.f, eps = 0.f;
+      if (e < br.y) {
+        j = s.bond_j[br.x + e];
+        r0 = s.bond_r0[br.x + e];
+        t = 0;
+      } else if (e < nba) {
+        j = s.ang_j[ar.x + e - br.y];
+        t = 1;
+      } else {
+        const float4 q = s.pl_att[abase + e - nba];
+        j = __float_as_int(q.x);
+        r0 = q.y;
+        eps = q.z;
+        t = 2;
+      }
+      const float4 xj = X(j);
+      float lx, ly, lz;
+      float dx = diff_exact(xj.x, xi.x, lx), dy = diff_exact(xj.y, xi.y, ly),
+            dz = diff_exact(xj.z, xi.z, lz);
+      if (wrap) min_image3(dx, dy, dz, boxl);
+      const float cc = small_coeff(s, t, dx, dy, dz, lx, ly, lz, r0, eps, fene_bad);
+      acc3(ax[c], ay[c], az[c], cc, dx, dy, dz);
+    }
+  }
+
+  // Non-native repulsion (energy.cu:536-581): co1 = -6 eps / d^2 (2 (s/r)^12 +
+  // (s/r)^6) [rep6: -6 eps / d^2 (s/r)^6]; pairs with d^2 <= 1e-7 sigma are
+  // skipped.  kC loads in flight per lane per chunk of kV entries.  A system
+  // of one bead type (UNI) uses its sigma as a constant.
+  const int ti = type_of(xi);
+  const float g11 = s.sig2[1][1], g12 = s.sig2[1][2], g22 = s.sig2[2][2];
+  const float t11 = s.rep_tol[1][1], t12 = s.rep_tol[1][2], t22 = s.rep_tol[2][2];
+  const float ce = -6.0f * s.eps_rep;
+  const float two = s.rep6 ? 0.0f : 2.0f;
+  const float q4 = 0.25f * boxl;
+  // pair-list partners are stored relative to the molecule's first bead
+  const unsigned short* __restrict__ prow = s.pl_j + rbase;
+  const int jbase = s.mol[m1].start;
+  for (int base = 0; base < rcnt; base += kV) {
+    int jj[kC];
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+      const int e = base + lane + c * G;
+      jj[c] = e < rcnt ? jbase + (int)prow[e] : i;
+    }
+    float4 xx[kC];
+#pragma unroll
+    for (int c = 0; c < kC; ++c) xx[c] = X(jj[c]);
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+      // past the row end xx[c] is bead i itself: d2 = 0 fails the tolerance
+      // test and contributes exactly 0, so no branch is needed
+      float dx = __fsub_rn(xx[c].x, xi.x), dy = __fsub_rn(xx[c].y, xi.y),
+            dz = __fsub_rn(xx[c].z, xi.z);
+      // |dx| + |dy| + |dz| bounds every component: one test for the rare wrap
+      if (wrap && fabsf(dx) + fabsf(dy) + fabsf(dz) > q4) min_image3(dx, dy, dz, boxl);
+      const float d2 = d2_plain(dx, dy, dz);
+      float sg2 = g11, tol = t11;
+      if (!UNI) {
+        const int tj = type_of(xx[c]);
+        sg2 = pick_type_pair(g11, g12, g22, ti, tj);
+        tol = pick_type_pair(t11, t12, t22, ti, tj);
+      }
+      const float inv = __fdividef(1.0f, d2);
+      const float u = __fmul_rn(sg2, inv);
+      const float u3 = __fmul_rn(__fmul_rn(u, u), u);
+      const float cc = (d2 > tol) ? __fmul_rn(__fmul_rn(__fmul_rn(ce, inv), u3), __fmaf_rn(two, u3, 1.0f))
+                                  : 0.0f;
+      acc3(ax[c], ay[c], az[c], cc, dx, dy, dz);
+    }
+  }
+  // upper levels of the fixed tree inside the lane, lower levels by shuffles
+#pragma unroll
+  for (int off = kV / 2; off >= G; off >>= 1) {
+    const int oc = off / G;
+#pragma unroll
+    for (int c = 0; c < kC; ++c)
+      if (c < oc) {
+        ax[c] = __fadd_rn(ax[c], ax[c + oc]);
+        ay[c] = __fadd_rn(ay[c], ay[c + oc]);
+        az[c] = __fadd_rn(az[c], az[c + oc]);
+      }
+  }
+#pragma unroll
+  for (int off = G / 2; off > 0; off >>= 1) {
+    ax[0] = __fadd_rn(ax[0], __shfl_xor_sync(gmask, ax[0], off));
+    ay[0] = __fadd_rn(ay[0], __shfl_xor_sync(gmask, ay[0], off));
+    az[0] = __fadd_rn(az[0], __shfl_xor_sync(gmask, az[0], off));
+  }
+  fene_bad = __any_sync(gmask, fene_bad);
+  fx = ax[0];
+  fy = ay[0];
+  fz = az[0];
+}
+
 // SPLIT = false: one kernel -- the groups' sums go through shared memory to
 // one thread per bead, which completes the step (finish_bead).  SPLIT = true:
 // the sums go to s.fsum and k_finish completes the step in a second launch
 // (no block barrier, coalesced state access; faster for large contexts).
 // Both complete a bead with the same finish_bead, so the results are the
 // same bits.
-template <int G, bool STEP, bool UNI, bool SPLIT>
-__global__ void __launch_bounds__(kStepThreads, StepBlocks<G>::value) k_step(DevSys s, int koff) {
+//
+// WIN = true: the block first stages the coordinates of the molecules its
+// beads belong to -- the contiguous bead range from the first bead's
+// molecule start to the last bead's molecule end, every bead from its own
+// molecule's current buffer -- into dynamic shared memory (up to wcap beads),
+// with coalesced loads; every partner of a bead lies in its own molecule, so
+// all gathers of the force sum then hit shared memory instead of L2.  A block
+// whose range exceeds wcap (or holds a free slot) gathers from global memory.
+// What a lane group needs about its bead slot b1 for step mol_step + STEP +
+// koff: the bead (-1: nothing to do -- a free slot, an inactive, failed,
+// finished or not yet started molecule), its molecule, the step and its row
+// descriptors.
+struct BeadSlot {
+  int i = -1, m1 = -1;
+  long long n = 0;
+  int2 br = make_int2(0, 0), ar = make_int2(0, 0);
+  int abase = 0, acnt = 0, rcnt = 0;
+};
+
+template <bool STEP>
+__device__ __forceinline__ BeadSlot bead_slot(const DevSys& s, int b1, int koff) {
+  BeadSlot q;
+  const bool live = b1 < s.nlive && !(*s.flags & FLAG_NL_OVERFLOW);
+  q.m1 = live ? s.mol_of[b1] : -1;  // -1: a free slot
+  // Row descriptors, loaded beside the molecule's state rather than after
+  // its test: they do not depend on it.
+  if (live) {
+    q.br = s.bond_row[b1];
+    q.ar = s.ang_row[b1];
+    q.abase = s.nat_row[b1].x;
+    q.acnt = s.pl_att_cnt[b1];
+    q.rcnt = s.pl_cnt[b1];
+  }
+  if (q.m1 >= 0) {
+    const MolConst& mc = s.mol[q.m1];
+    q.n = s.mol_step[q.m1] + (STEP ? 1 : 0) + koff;
+    // n < 0: a molecule admitted to a running context whose step 0 comes later
+    // in this block; n > nsteps: finished
+    if (mc.active && s.mol_status[q.m1] == 0 && q.n >= 0 &&
+        !(STEP && mc.nsteps >= 0 && q.n > mc.nsteps))
+      q.i = b1;
+  }
+  return q;
+}
+
+// The force sum's w: the marker bits of finish_bead (summed, a bond past R0,
+// the parity of the step, which selects the coordinate buffers).
+__device__ __forceinline__ float4 marked_sum(float fx, float fy, float fz, bool fene_bad,
+                                             long long n) {
+  return make_float4(fx, fy, fz,
+                     __int_as_float(kSummed | (fene_bad ? kFeneBad : 0) |
+                                    ((int)(n & 1) ? kOddStep : 0)));
+}
+
+template <int G, bool STEP, bool UNI, bool SPLIT, bool WIN>
+__global__ void __launch_bounds__(kStepThreads, StepBlocks<G>::value) k_step(DevSys s, int koff,
+                                                                            int wcap) {
   constexpr int BPB = kStepThreads / G;  // beads per block
+  extern __shared__ float4 xwin[];
+  __shared__ int win_lo, win_n;          // window start bead and length (-1: none)
   pdl_wait();
   pdl_release();
   const int slot = threadIdx.x / G;
   const int lane = threadIdx.x % G;
-  int i = -1;
-  long long n = 0;
   const int b1 = blockIdx.x * BPB + slot;
-  const bool live = b1 < s.nlive && !(*s.flags & FLAG_NL_OVERFLOW);
-  const int m1 = live ? s.mol_of[b1] : -1;  // -1: a free slot
-  // Row descriptors, loaded beside the molecule's state rather than after
-  // its test: they do not depend on it.
-  int2 br = make_int2(0, 0), ar = make_int2(0, 0);
-  int abase = 0, acnt = 0, rcnt = 0;
-  if (live) {
-    br = s.bond_row[b1];
-    ar = s.ang_row[b1];
-    abase = s.nat_row[b1].x;
-    acnt = s.pl_att_cnt[b1];
-    rcnt = s.pl_cnt[b1];
+  const BeadSlot q = bead_slot<STEP>(s, b1, koff);
+  const int i = q.i, m1 = q.m1;
+  const long long n = q.n;
+  if (WIN) {
+    if (threadIdx.x == 0) {
+      int lo = 0, len = -1;
+      const int b0 = blockIdx.x * BPB;
+      const int bl = min(b0 + BPB, s.nlive) - 1;
+      if (b0 <= bl && !(*s.flags & FLAG_NL_OVERFLOW)) {
+        const int m0 = s.mol_of[b0], ml = s.mol_of[bl];
+        if (m0 >= 0 && ml >= 0) {
+          lo = s.mol[m0].start;
+          const int hi = s.mol[ml].start + s.mol[ml].n;
+          if (hi - lo <= wcap) len = hi - lo;
+        }
+      }
+      win_lo = lo;
+      win_n = len;
+    }
+    __syncthreads();
+    const int lo = win_lo, len = win_n;
+    for (int k = threadIdx.x; k < len; k += kStepThreads) {
+      const int b = lo + k;
+      const int m = s.mol_of[b];
+      const int par = m >= 0 ? (int)((s.mol_step[m] + (STEP ? 1 : 0) + koff) & 1) : 0;
+      xwin[k] = s.x[par][b];
+    }
+    __syncthreads();
   }
-  if (m1 >= 0) {
-    const MolConst& mc = s.mol[m1];
-    n = s.mol_step[m1] + (STEP ? 1 : 0) + koff;
-    // n < 0: a molecule admitted to a running context whose step 0 comes later
-    // in this block; n > nsteps: finished
-    if (mc.active && s.mol_status[m1] == 0 && n >= 0 && !(STEP && mc.nsteps >= 0 && n > mc.nsteps))
-      i = b1;
-  }
-  // Forces are summed in a fixed order whatever G is: entry e of a row
-  // accumulates into virtual lane e % kV (in increasing e), and the kV partial
-  // sums combine in one fixed binary tree (pairs v, v + kV/2, then v, v + kV/4,
-  // ...).  Each physical lane holds kC = kV / G virtual lanes and does the
-  // upper tree levels locally, the rest by shuffles.  So every G gives
-  // bit-identical forces, and G is free to tune per context.
-  constexpr int kC = kV / G;
-  float ax[kC], ay[kC], az[kC];
-#pragma unroll
-  for (int c = 0; c < kC; ++c) ax[c] = ay[c] = az[c] = 0.f;
+  float fx = 0.f, fy = 0.f, fz = 0.f;
   bool fene_bad = false;
   if (i >= 0) {  // uniform over the lane group
-    const unsigned gmask = (G == 32) ? 0xffffffffu
-                                     : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
-    const float4* __restrict__ X = s.x[(int)(n & 1)];
-    const float4 xi = X[i];
-    const float boxl = s.boxl;
-    // 0 when no pair of the molecule can reach boxl/4 (from its last binning,
-    // with a cut-off of margin): the minimum image is then the identity and
-    // its test is skipped
-    const bool wrap = s.grid[m1].wrap != 0;
-    const long long rbase = (long long)i * s.nl_stride;
-
-    // Bonded, angle and native terms share one index space [bonds | angles |
-    // natives]; a bead has a handful of them, usually one pass.
-    const int nba = br.y + ar.y;
-    const int nsmall = nba + acnt;
-    for (int base = 0; base < nsmall; base += kV) {
-#pragma unroll
-      for (int c = 0; c < kC; ++c) {
-        const int e = base + lane + c * G;
-        if (e >= nsmall) continue;
-        int j, t;
-        float r0 = 0.f, eps = 0.f;
-        if (e < br.y) {
-          j = s.bond_j[br.x + e];
-          r0 = s.bond_r0[br.x + e];
-          t = 0;
-        } else if (e < nba) {
-          j = s.ang_j[ar.x + e - br.y];
-          t = 1;
-        } else {
-          const float4 q = s.pl_att[abase + e - nba];
-          j = __float_as_int(q.x);
-          r0 = q.y;
-          eps = q.z;
-          t = 2;
-        }
-        const float4 xj = X[j];
-        float lx, ly, lz;
-        float dx = diff_exact(xj.x, xi.x, lx), dy = diff_exact(xj.y, xi.y, ly),
-              dz = diff_exact(xj.z, xi.z, lz);
-        if (wrap) min_image3(dx, dy, dz, boxl);
-        const float cc = small_coeff(s, t, dx, dy, dz, lx, ly, lz, r0, eps, fene_bad);
-        acc3(ax[c], ay[c], az[c], cc, dx, dy, dz);
-      }
+    if (WIN && win_n >= 0) {
+      bead_force<G, UNI>(s, WindowX{xwin, win_lo}, i, m1, lane, q.br, q.ar, q.abase, q.acnt,
+                         q.rcnt, fx, fy, fz, fene_bad);
+    } else {
+      bead_force<G, UNI>(s, GlobalX{s.x[(int)(n & 1)]}, i, m1, lane, q.br, q.ar, q.abase, q.acnt,
+                         q.rcnt, fx, fy, fz, fene_bad);
     }
-
-    // Non-native repulsion (energy.cu:536-581): co1 = -6 eps / d^2 (2 (s/r)^12 +
-    // (s/r)^6) [rep6: -6 eps / d^2 (s/r)^6]; pairs with d^2 <= 1e-7 sigma are
-    // skipped.  kC loads in flight per lane per chunk of kV entries.  A system
-    // of one bead type (UNI) uses its sigma as a constant.
-    const int ti = type_of(xi);
-    const float g11 = s.sig2[1][1], g12 = s.sig2[1][2], g22 = s.sig2[2][2];
-    const float t11 = s.rep_tol[1][1], t12 = s.rep_tol[1][2], t22 = s.rep_tol[2][2];
-    const float ce = -6.0f * s.eps_rep;
-    const float two = s.rep6 ? 0.0f : 2.0f;
-    const float q4 = 0.25f * boxl;
-    const int* __restrict__ prow = s.pl_j + rbase;
-    for (int base = 0; base < rcnt; base += kV) {
-      int jj[kC];
-#pragma unroll
-      for (int c = 0; c < kC; ++c) {
-        const int e = base + lane + c * G;
-        jj[c] = e < rcnt ? prow[e] : i;
-      }
-      float4 xx[kC];
-#pragma unroll
-      for (int c = 0; c < kC; ++c) xx[c] = X[jj[c]];
-#pragma unroll
-      for (int c = 0; c < kC; ++c) {
-        // past the row end xx[c] is bead i itself: d2 = 0 fails the tolerance
-        // test and contributes exactly 0, so no branch is needed
-        float dx = __fsub_rn(xx[c].x, xi.x), dy = __fsub_rn(xx[c].y, xi.y),
-              dz = __fsub_rn(xx[c].z, xi.z);
-        // |dx| + |dy| + |dz| bounds every component: one test for the rare wrap
-        if (wrap && fabsf(dx) + fabsf(dy) + fabsf(dz) > q4) min_image3(dx, dy, dz, boxl);
-        const float d2 = d2_plain(dx, dy, dz);
-        float sg2 = g11, tol = t11;
-        if (!UNI) {
-          const int tj = type_of(xx[c]);
-          sg2 = pick_type_pair(g11, g12, g22, ti, tj);
-          tol = pick_type_pair(t11, t12, t22, ti, tj);
-        }
-        const float inv = __fdividef(1.0f, d2);
-        const float u = __fmul_rn(sg2, inv);
-        const float u3 = __fmul_rn(__fmul_rn(u, u), u);
-        const float cc = (d2 > tol) ? __fmul_rn(__fmul_rn(__fmul_rn(ce, inv), u3), __fmaf_rn(two, u3, 1.0f))
-                                    : 0.0f;
-        acc3(ax[c], ay[c], az[c], cc, dx, dy, dz);
-      }
-    }
-    // upper levels of the fixed tree inside the lane, lower levels by shuffles
-#pragma unroll
-    for (int off = kV / 2; off >= G; off >>= 1) {
-      const int oc = off / G;
-#pragma unroll
-      for (int c = 0; c < kC; ++c)
-        if (c < oc) {
-          ax[c] = __fadd_rn(ax[c], ax[c + oc]);
-          ay[c] = __fadd_rn(ay[c], ay[c + oc]);
-          az[c] = __fadd_rn(az[c], az[c + oc]);
-        }
-    }
-#pragma unroll
-    for (int off = G / 2; off > 0; off >>= 1) {
-      ax[0] = __fadd_rn(ax[0], __shfl_xor_sync(gmask, ax[0], off));
-      ay[0] = __fadd_rn(ay[0], __shfl_xor_sync(gmask, ay[0], off));
-      az[0] = __fadd_rn(az[0], __shfl_xor_sync(gmask, az[0], off));
-    }
-    fene_bad = __any_sync(gmask, fene_bad);
   }
-  // w: the marker bits of finish_bead (summed, a bond past R0, the parity of
-  // the step, which selects the coordinate buffers)
-  const float4 sum = make_float4(ax[0], ay[0], az[0],
-                                 __int_as_float(kSummed | (fene_bad ? kFeneBad : 0) |
-                                                ((int)(n & 1) ? kOddStep : 0)));
+  const float4 sum = marked_sum(fx, fy, fz, fene_bad, n);
   if (SPLIT) {
     // the group's sum, marked for k_finish (which completes the step)
     if (i >= 0 && lane == 0) s.fsum[i] = sum;
@@ -343,6 +438,118 @@ __global__ void __launch_bounds__(256, 6) k_finish(DevSys s, int koff) {
   finish_bead<STEP>(s, b, m, fs, koff);
 }
 
+// ------------------------------------------------------ persistent form
+// Every step of a run of steps with no list rebuild in between, in one
+// cooperative launch: each block owns bead chunks (grid-stride) and completes
+// them step after step, with a device-wide barrier between steps (x_{n+1} of
+// every bead is written before any bead's force of step n+1 reads it).  The
+// per-bead code is k_step's one-kernel form, so the bits are the same.
+//
+// The barrier: bar[0] counts the blocks that arrived, bar[1] is the
+// generation.  The last block to arrive resets the count and advances the
+// generation; the others wait for it with a time limit, after which they set
+// FLAG_BARRIER_TIMEOUT and the whole launch returns (the host reports the
+// context as failed and clears the count).  `expected` is the number of
+// arrivals that complete the barrier: gridDim.x, or more for the check that
+// makes the wait run out on purpose.
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Called by every thread of the block; returns false on a timed-out wait.
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned expected, unsigned& gen,
+                                             unsigned long long limit_ns, int* flags) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int good = 1;
+    __threadfence();
+    if (atomicAdd(&bar[0], 1u) + 1u == expected) {
+      atomicExch(&bar[0], 0u);
+      __threadfence();
+      atomicAdd(&bar[1], 1u);
+    } else {
+      const unsigned long long t0 = global_ns();
+      while (ld_acquire_gpu(&bar[1]) == gen) {
+        if (global_ns() - t0 > limit_ns) {
+          good = 0;
+          atomicOr(flags, FLAG_BARRIER_TIMEOUT);
+          break;
+        }
+        __nanosleep(100);
+      }
+      __threadfence();
+    }
+    ++gen;
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+template <int G, bool STEP, bool UNI>
+__global__ void __launch_bounds__(kStepThreads, StepBlocks<G>::value)
+    k_step_persist(DevSys s, int koff0, int count,
+                                                               unsigned* bar, unsigned expected,
+                                                               unsigned long long limit_ns) {
+  constexpr int BPB = kStepThreads / G;
+  __shared__ float4 fsum[BPB];
+  __shared__ int bead[BPB];
+  __shared__ unsigned gen0;
+  pdl_wait();
+  pdl_release();
+  // every block reads the generation before it first arrives, so all agree
+  if (threadIdx.x == 0) gen0 = ld_acquire_gpu(&bar[1]);
+  __syncthreads();
+  unsigned gen = gen0;
+  const int slot = threadIdx.x / G;
+  const int lane = threadIdx.x % G;
+  const int nchunks = (s.nlive + BPB - 1) / BPB;
+  for (int k = 0; k < count; ++k) {
+    if (k > 0 && !grid_barrier(bar, expected, gen, limit_ns, s.flags)) return;
+    const int koff = koff0 + k;
+    for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+      const BeadSlot q = bead_slot<STEP>(s, c * BPB + slot, koff);
+      float fx = 0.f, fy = 0.f, fz = 0.f;
+      bool fene_bad = false;
+      if (q.i >= 0)
+        bead_force<G, UNI>(s, GlobalX{s.x[(int)(q.n & 1)]}, q.i, q.m1, lane, q.br, q.ar, q.abase,
+                           q.acnt, q.rcnt, fx, fy, fz, fene_bad);
+      if (lane == 0) {
+        fsum[slot] = marked_sum(fx, fy, fz, fene_bad, q.n);
+        bead[slot] = q.i;
+      }
+      __syncthreads();
+      if (threadIdx.x < BPB) {
+        const int b = bead[threadIdx.x];
+        if (b >= 0) finish_bead<STEP>(s, b, s.mol_of[b], fsum[threadIdx.x], koff);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// The barrier alone, for the check that its wait ends: `rounds` barriers
+// with `expected` arrivals (gridDim.x completes them; more makes every block
+// wait out the limit).
+__global__ void k_barrier_check(DevSys s, unsigned* bar, unsigned expected, int rounds,
+                                unsigned long long limit_ns) {
+  __shared__ unsigned gen0;
+  if (threadIdx.x == 0) gen0 = ld_acquire_gpu(&bar[1]);
+  __syncthreads();
+  unsigned gen = gen0;
+  for (int r = 0; r < rounds; ++r)
+    if (!grid_barrier(bar, expected, gen, limit_ns, s.flags)) return;
+}
+
 // End of a block of `steps` steps: advance each running molecule's step
 // count (clamped to its budget).  A neighbour-list overflow freezes
 // everything until the host regrows the list and re-runs the block.
@@ -412,8 +619,9 @@ __global__ void __launch_bounds__(256) k_energy(DevSys s, int mol_start, int mol
     const long long rbase = (long long)i * s.nl_stride;
     const int rcnt = s.pl_cnt[i];
     const int ti = type_of(xi);
+    const int jbase = s.mol[m].start;
     for (int e = 0; e < rcnt; ++e) {
-      const float4 xj = X[s.pl_j[rbase + e]];
+      const float4 xj = X[jbase + (int)s.pl_j[rbase + e]];
       float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
       min_image3(dx, dy, dz, boxl);
       float u = s.sig2[ti][type_of(xj)] / (dx * dx + dy * dy + dz * dz);
@@ -525,16 +733,17 @@ __global__ void k_gather_current(DevSys s, float* __restrict__ out, int* __restr
 // ----------------------------------------------------------- launchers
 static inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
-template <int G, bool SPLIT>
-static void launch_step_gs(const DevSys& s, int koff, bool step, cudaStream_t st) {
+template <int G, bool SPLIT, bool WIN>
+static void launch_step_gsw(const DevSys& s, int koff, bool step, int wcap, cudaStream_t st) {
   const unsigned blocks = cdiv(s.nlive, kStepThreads / G);
   const int T = kStepThreads;
+  const size_t sm = WIN ? (size_t)wcap * sizeof(float4) : 0;
   if (s.uniform_type) {
-    if (step) launch_pdl(k_step<G, true, true, SPLIT>, blocks, T, st, s, koff);
-    else launch_pdl(k_step<G, false, true, SPLIT>, blocks, T, st, s, koff);
+    if (step) launch_pdl_smem(k_step<G, true, true, SPLIT, WIN>, blocks, T, sm, st, s, koff, wcap);
+    else launch_pdl_smem(k_step<G, false, true, SPLIT, WIN>, blocks, T, sm, st, s, koff, wcap);
   } else {
-    if (step) launch_pdl(k_step<G, true, false, SPLIT>, blocks, T, st, s, koff);
-    else launch_pdl(k_step<G, false, false, SPLIT>, blocks, T, st, s, koff);
+    if (step) launch_pdl_smem(k_step<G, true, false, SPLIT, WIN>, blocks, T, sm, st, s, koff, wcap);
+    else launch_pdl_smem(k_step<G, false, false, SPLIT, WIN>, blocks, T, sm, st, s, koff, wcap);
   }
   if (SPLIT) {
     if (step) launch_pdl(k_finish<true>, cdiv(s.nlive, 256), 256, st, s, koff);
@@ -543,19 +752,129 @@ static void launch_step_gs(const DevSys& s, int koff, bool step, cudaStream_t st
 }
 
 template <int G>
-static void launch_step_g(const DevSys& s, bool split, int koff, bool step, cudaStream_t st) {
-  if (split) launch_step_gs<G, true>(s, koff, step, st);
-  else launch_step_gs<G, false>(s, koff, step, st);
+static void launch_step_g(const DevSys& s, bool split, int koff, bool step, int wcap,
+                          cudaStream_t st) {
+  if (wcap > 0) {
+    if (split) launch_step_gsw<G, true, true>(s, koff, step, wcap, st);
+    else launch_step_gsw<G, false, true>(s, koff, step, wcap, st);
+  } else {
+    if (split) launch_step_gsw<G, true, false>(s, koff, step, 0, st);
+    else launch_step_gsw<G, false, false>(s, koff, step, 0, st);
+  }
 }
 
-// Lanes per bead G in {2, 4, 8, 16}; split: force kernel + finish kernel.
-void launch_step(const DevSys& s, int G, bool split, int koff, bool step, cudaStream_t st) {
+// Lanes per bead G in {2, 4, 8, 16}; split: force kernel + finish kernel;
+// wcap > 0: stage each block's molecules (up to wcap beads) in shared memory.
+void launch_step(const DevSys& s, int G, bool split, int koff, bool step, int wcap,
+                 cudaStream_t st) {
   switch (G) {
-    case 2: launch_step_g<2>(s, split, koff, step, st); break;
-    case 4: launch_step_g<4>(s, split, koff, step, st); break;
-    case 16: launch_step_g<16>(s, split, koff, step, st); break;
-    default: launch_step_g<8>(s, split, koff, step, st); break;
+    case 2: launch_step_g<2>(s, split, koff, step, wcap, st); break;
+    case 4: launch_step_g<4>(s, split, koff, step, wcap, st); break;
+    case 16: launch_step_g<16>(s, split, koff, step, wcap, st); break;
+    default: launch_step_g<8>(s, split, koff, step, wcap, st); break;
   }
+}
+
+// Cooperative launch: every block is resident at once (the barrier needs it).
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_coop(void (*kernel)(KArgs...), unsigned grid, unsigned block,
+                               cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+// Blocks of the persistent form (lanes G, step or force-only, one bead type
+// or two) that are resident at once on this device, at most one per chunk.
+template <int G, bool STEP, bool UNI>
+static int persist_grid(int nchunks) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_step_persist<G, STEP, UNI>, kStepThreads,
+                                                0);
+  const int resident = std::max(1, per) * std::max(1, sms);
+  return std::max(1, std::min(resident, nchunks));
+}
+
+template <int G, bool STEP, bool UNI>
+static cudaError_t launch_persist_gsu(const DevSys& s, int koff0, int count, unsigned* bar,
+                                      unsigned long long limit_ns, cudaStream_t st) {
+  const unsigned grid = (unsigned)persist_grid<G, STEP, UNI>((int)cdiv(s.nlive, kStepThreads / G));
+  return launch_coop(k_step_persist<G, STEP, UNI>, grid, kStepThreads, st, s, koff0, count, bar,
+                     grid, limit_ns);
+}
+
+template <int G>
+static cudaError_t launch_persist_g(const DevSys& s, int koff0, int count, bool step,
+                                    unsigned* bar, unsigned long long limit_ns, cudaStream_t st) {
+  if (s.uniform_type) {
+    if (step) return launch_persist_gsu<G, true, true>(s, koff0, count, bar, limit_ns, st);
+    return launch_persist_gsu<G, false, true>(s, koff0, count, bar, limit_ns, st);
+  }
+  if (step) return launch_persist_gsu<G, true, false>(s, koff0, count, bar, limit_ns, st);
+  return launch_persist_gsu<G, false, false>(s, koff0, count, bar, limit_ns, st);
+}
+
+// Steps koff0 .. koff0 + count - 1 (no list rebuild among them) in one
+// cooperative launch; bar: the context's two barrier words.
+cudaError_t launch_step_persist(const DevSys& s, int G, int koff0, int count, bool step,
+                                unsigned* bar, unsigned long long limit_ns, cudaStream_t st) {
+  switch (G) {
+    case 2: return launch_persist_g<2>(s, koff0, count, step, bar, limit_ns, st);
+    case 4: return launch_persist_g<4>(s, koff0, count, step, bar, limit_ns, st);
+    case 16: return launch_persist_g<16>(s, koff0, count, step, bar, limit_ns, st);
+    default: return launch_persist_g<8>(s, koff0, count, step, bar, limit_ns, st);
+  }
+}
+
+// `rounds` barriers over the persistent form's grid with `missing` arrivals
+// that never come (0: the barriers complete).
+cudaError_t launch_barrier_check(const DevSys& s, int G, unsigned* bar, int missing, int rounds,
+                                 unsigned long long limit_ns, cudaStream_t st) {
+  const int nchunks = (int)cdiv(s.nlive, kStepThreads / G);
+  int grid = 1;
+  switch (G) {
+    case 2: grid = persist_grid<2, true, true>(nchunks); break;
+    case 4: grid = persist_grid<4, true, true>(nchunks); break;
+    case 16: grid = persist_grid<16, true, true>(nchunks); break;
+    default: grid = persist_grid<8, true, true>(nchunks); break;
+  }
+  return launch_coop(k_barrier_check, (unsigned)grid, kStepThreads, st, s, bar,
+                     (unsigned)grid + (unsigned)missing, rounds, limit_ns);
+}
+
+// Opts every windowed step kernel in to wcap beads of dynamic shared memory
+// (above the 48 KB default a kernel must ask for it).
+template <int G>
+static cudaError_t allow_window_g(int wcap) {
+  const int bytes = wcap * (int)sizeof(float4);
+  cudaError_t e = cudaSuccess;
+#define SOP_ALLOW(STEP, UNI, SPLIT)                                                           \
+  if (e == cudaSuccess)                                                                       \
+    e = cudaFuncSetAttribute(k_step<G, STEP, UNI, SPLIT, true>,                               \
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  SOP_ALLOW(true, true, true) SOP_ALLOW(true, true, false) SOP_ALLOW(true, false, true)
+  SOP_ALLOW(true, false, false) SOP_ALLOW(false, true, true) SOP_ALLOW(false, true, false)
+  SOP_ALLOW(false, false, true) SOP_ALLOW(false, false, false)
+#undef SOP_ALLOW
+  return e;
+}
+
+cudaError_t allow_step_window(int wcap) {
+  cudaError_t e = allow_window_g<2>(wcap);
+  if (e == cudaSuccess) e = allow_window_g<4>(wcap);
+  if (e == cudaSuccess) e = allow_window_g<8>(wcap);
+  if (e == cudaSuccess) e = allow_window_g<16>(wcap);
+  return e;
 }
 
 void launch_gather_current(const DevSys& s, float* out, int* flag_out, cudaStream_t st) {

@@ -93,7 +93,9 @@ struct DevSys {
   int* pl_att_cnt; float4* pl_att;
   int* nl_cnt; int* nl_j; long long nl_stride;
   int* nl_maxrow;               // largest row a rebuild needed (for regrowth)
-  int* pl_cnt; int* pl_j;
+  int* pl_cnt;
+  unsigned short* pl_j;         // repulsive PL rows: partner - molecule start (molecules
+                                // hold at most 65,535 beads), same row stride as nl_j
 
   // neighbour-list build scratch
   unsigned* bbox;               // 6 per molecule, order-preserving float bits
@@ -105,7 +107,7 @@ struct DevSys {
   int use_noise;
 };
 
-enum { FLAG_NL_OVERFLOW = 1 };
+enum { FLAG_NL_OVERFLOW = 1, FLAG_BARRIER_TIMEOUT = 2 };
 
 // --------------------------------------------------------------- helpers
 // Programmatic dependent launch.  The per-step kernels are launched with
@@ -128,6 +130,22 @@ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), unsigned grid, unsigned 
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(block);
   cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+// The same with dynamic shared memory.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl_smem(void (*kernel)(KArgs...), unsigned grid, unsigned block,
+                                   size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;

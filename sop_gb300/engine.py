@@ -51,7 +51,8 @@ class Params(ctypes.Structure):
                 ("nnlup", ctypes.c_int), ("nplup", ctypes.c_int), ("rep6", ctypes.c_int),
                 ("device", ctypes.c_int), ("graph_steps", ctypes.c_int),
                 ("lanes_per_bead", ctypes.c_int), ("seed", ctypes.c_ulonglong),
-                ("integrator", ctypes.c_int), ("step_split", ctypes.c_int)]
+                ("integrator", ctypes.c_int), ("step_split", ctypes.c_int),
+                ("step_window", ctypes.c_int)]
 
 
 class MoleculeDesc(ctypes.Structure):
@@ -141,6 +142,8 @@ def lib() -> ctypes.CDLL:
                                      ctypes.POINTER(ctypes.c_double)]),
             "sop_serve_stats": (I, [V, V]),
             "sop_step_form": (I, [V, ctypes.POINTER(I), ctypes.POINTER(I)]),
+            "sop_step_window": (I, [V, ctypes.POINTER(I)]),
+            "sop_check_step_barrier": (I, [V, I, ctypes.c_double, ctypes.POINTER(I)]),
             "sop_checkpoint": (I, [V, I, V, LL, PLL]),
             "sop_restore": (I, [V, I, V, LL]),
             "sop_serve_checkpoint": (I, [V, I, V, LL, PLL]),
@@ -369,8 +372,18 @@ class Engine:
         self._check(lib().sop_tuning(self.h, ctypes.byref(g), _p(ms)), self.h)
         form = ctypes.c_int()
         self._check(lib().sop_step_form(self.h, None, ctypes.byref(form)), self.h)
-        return {"lanes_per_bead": g.value, "form": form.value,
+        win = ctypes.c_int()
+        self._check(lib().sop_step_window(self.h, ctypes.byref(win)), self.h)
+        return {"lanes_per_bead": g.value, "form": form.value, "window": win.value,
                 "ms": {str(k): float(v) for k, v in zip((2, 4, 8, 16), ms)}}
+
+    def check_step_barrier(self, missing: int, timeout_s: float) -> bool:
+        """Runs the persistent step's device-wide barrier with `missing`
+        arrivals that never come; True when a wait ran out."""
+        t = ctypes.c_int()
+        self._check(lib().sop_check_step_barrier(self.h, int(missing), float(timeout_s),
+                                                 ctypes.byref(t)), self.h)
+        return bool(t.value)
 
     def stream(self) -> int:
         s = ctypes.c_void_p()

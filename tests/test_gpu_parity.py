@@ -372,13 +372,14 @@ def test_batched_equals_alone():
 
 def test_lanes_per_bead_bit_identical():
     """The force summation order does not depend on the lanes per bead, and
-    both forms of the step (one kernel; force + finish kernels) complete a
-    bead with the same code, so trajectories are bit-identical for every G
-    and form (both can be tuned freely)."""
+    every form of the step (one kernel; force + finish kernels; the steps
+    between two rebuilds in one persistent launch) completes a bead with the
+    same code, so trajectories are bit-identical for every G and form (both
+    can be tuned freely)."""
     mol = mol_of(4000, 1)
     outs = []
     for g in (2, 4, 8, 16):
-        for form in (1, 2):
+        for form in (1, 2, 3):
             p = engine.baseline_params(lanes_per_bead=g, step_split=form)
             with engine.plain(mol, mol.xyz, p, T=0.6, traj=2) as e:
                 t = e.tuning()
@@ -390,11 +391,63 @@ def test_lanes_per_bead_bit_identical():
             np.testing.assert_array_equal(o[k], outs[0][k])
 
 
+def test_step_window_bit_identical():
+    """Blocks that stage their molecules in shared memory gather the same
+    coordinates as blocks that read global memory, in the same order: a
+    batched context of molecules from 40 to 1,800 beads (some blocks fit a
+    window, some do not; two bead types in one molecule) steps bit-identically
+    with no window, small and large windows, every form and several G."""
+    mols = [mol_of(n, 30 + k) for k, n in enumerate((40, 300, 1800, 75, 900, 1200, 60))]
+    base = mols[3]
+    types = np.where(np.arange(base.n) % 3 == 0, 2, 1).astype(np.int32)
+    mols[3] = system.Molecule(base.n, base.xyz, base.bond_i, base.bond_j, base.bond_r0,
+                              base.ang_i, base.ang_j, base.ang_k, base.ang_r, base.nat_i,
+                              base.nat_j, base.nat_r0, base.nat_eps, types=types)
+    outs = []
+    for win in (-1, 256, 1024, 2048):
+        for g, form in ((4, 1), (8, 2), (16, 1), (8, 3)):
+            p = engine.baseline_params(lanes_per_bead=g, step_split=form, step_window=win)
+            e = engine.Engine(p)
+            for k, m in enumerate(mols):
+                e.add(m, m.xyz, T=0.6, traj=k)
+            e.commit()
+            t = e.tuning()
+            assert t["window"] == max(win, 0) and t["lanes_per_bead"] == g
+            e.step(60)
+            outs.append([e.download(k) for k in range(len(mols))])
+            e.close()
+    for o in outs[1:]:
+        for k in range(len(mols)):
+            for key in ("unc_pos", "vel", "force"):
+                np.testing.assert_array_equal(o[k][key], outs[0][k][key])
+
+
+def test_persistent_step_barrier_wait_ends():
+    """The persistent form's device-wide barrier completes when every block
+    arrives, and when an arrival never comes its wait runs out after the
+    limit: the kernel returns, the host reads the flag, and the context keeps
+    stepping exactly as a context that never saw it."""
+    mol = mol_of(4000, 1)
+    p = engine.baseline_params(lanes_per_bead=4, step_split=3)
+    with engine.plain(mol, mol.xyz, p, T=0.6, traj=3) as e, \
+            engine.plain(mol, mol.xyz, p, T=0.6, traj=3) as ref:
+        assert e.tuning()["form"] == 3
+        e.step(25)
+        assert e.check_step_barrier(0, 1.0) is False
+        assert e.check_step_barrier(1, 0.2) is True
+        assert e.check_step_barrier(0, 1.0) is False
+        e.step(25)
+        ref.step(50)
+        a, b = e.download(), ref.download()
+        for key in ("unc_pos", "vel", "force"):
+            np.testing.assert_array_equal(a[key], b[key])
+
+
 def test_autotune_picks_a_candidate():
     mol = mol_of(4000, 1)
     with engine.plain(mol, mol.xyz, engine.baseline_params()) as e:
         t = e.tuning()
-    assert t["lanes_per_bead"] in (2, 4, 8, 16) and t["form"] in (1, 2)
+    assert t["lanes_per_bead"] in (2, 4, 8, 16) and t["form"] in (1, 2, 3)
     assert all(v > 0 for v in t["ms"].values())
 
 

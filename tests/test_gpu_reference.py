@@ -9,8 +9,8 @@ reference's factor mode (3.2 / 2.5 x r0 or sigma).
 - lists: bit-exact as sets, every case (native, perturbed, extended, two
   bead types; 128 and 4,000 beads);
 - forces: the engine against the reference's kernels within the reference's
-  own FP32 error (REF_FORCE_TOL, the bound its kernels keep against FP64),
-  and against FP64 within 1e-5.
+  own FP32 error (the bounds its kernels keep against FP64:
+  test_golden.assert_force_close_to_reference), and against FP64 within 1e-5.
 """
 import os
 import sys
@@ -27,7 +27,7 @@ pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 sys.path.insert(0, GOLD)
 import cases  # noqa: E402
-from test_golden import REF_FORCE_TOL, assert_lists_equal  # noqa: E402
+from test_golden import assert_force_close_to_reference, assert_lists_equal  # noqa: E402
 
 
 def engine_for(name):
@@ -64,9 +64,8 @@ def test_engine_forces_match_reference_kernels(name):
         f = e.download()["force"]
         ai, aj, _ = e.list_pairs(0, 2)
         ri, rj, _ = e.list_pairs(0, 3)
-    err_ref = force_error(f, f_ref)
     f64, _ = O.forces_f64(mol, x, att_sel(mol, ai, aj), ri, rj, params={"boxl": boxl})
     err64 = force_error(f, f64)
-    print(name, "engine vs reference kernels:", err_ref, "engine vs FP64:", err64)
-    assert err_ref <= REF_FORCE_TOL, (name, err_ref)
+    print(name, "engine vs reference kernels:", force_error(f, f_ref), "engine vs FP64:", err64)
+    assert_force_close_to_reference(name, f, f_ref)
     assert err64 <= 1e-5, (name, err64)

@@ -1,4 +1,4 @@
-"""Long runs compared with the reference algorithm.
+"""Long runs compared with the reference.
 
 Same noise: the engine and the oracle's serial FP32 run of the reference
 loop (orc_ref_*: the reference's step order, sop.cu:197-278, with the same
@@ -6,77 +6,91 @@ Philox stream) start from the same structure; their trajectories agree to
 FP32 rounding for the first hundred steps and only then drift apart
 (molecular dynamics is chaotic).
 
-Independent seeds: the reference draws cuRAND XORWOW (energy.cu:588-604), so
-long trajectories cannot match step for step.  Independent seeds of the
-128-bead structure at kBT = 0.6 run on the GPU (one batched context, one
-Philox stream each) and on the oracle's reference run.  After an
-equilibration, each trajectory's time averages of the total energy, Rg^2 and
-the native-contact fraction Q are one sample; the two sets of per-seed means
-are compared by z = (mean_gpu - mean_ref) / combined standard error.  The
-acceptance criterion is |z| <= 2 for each of the three; a correct engine
-misses one 2-sigma check by chance about one time in twenty, and every
-change of the kernels' rounding redraws the trajectories, so the assertion
-is |z| <= 3 (about one build in a hundred) and the z values are printed
-for the record.  The same-noise comparison above is the deterministic pin
-of the dynamics.  The kinetic temperature must agree within 1%.
+Independent seeds, against the reference program itself: the reference's
+own binary (underdamped_ctrl with cuRAND XORWOW noise, GPU list drivers) ran
+its input script once per seed on the GPU (tests/golden/make_ref_stats.py;
+ref_stats.npz holds each run's time averages of rna_etot, Rg^2, Q and the
+kinetic temperature over steps 1,100 .. 5,000, sampled every 100 steps).  The
+engine runs the same structures in the reference's settings -- factor-mode
+cut-offs, neighbour list every 50 steps, pair list every step, kBT 0.6, the
+reference's native energy coefficient 0.7 -- with one Philox stream per seed
+and the same sampling.  Per observable, z = (mean_engine - mean_reference) /
+combined standard error of the per-run means must satisfy |z| <= 2 (the
+stated criterion); the kinetic temperature must agree within 1%.
+
+At h = 0.05 a FENE bond occasionally overshoots R0 in a long 4,000-bead run:
+3 of the reference's 48 runs produced a NaN energy (log of a negative
+argument, energy.cu:217-223) and one of them blew up.  The engine stops such
+a molecule with SOP_MOL_FENE_RANGE.  Runs that failed are left out on both
+sides, and the numbers of failed runs must agree within binomial noise.
 """
-from concurrent.futures import ThreadPoolExecutor
+import os
 
 import numpy as np
 import pytest
 
-from helpers import oracle_lists
 from oracle import pyoracle as O
 from sop_gb300 import engine, system
 
 pytestmark = pytest.mark.gpu
 
-SEEDS = 64
-EQUIL = 1000
-SAMPLES = 40
-EVERY = 100
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 T = 0.6
 CUT = [0.0, 32.0, 0.0, 32.0, 0.0, 16.0, 0.0, 16.0]   # the engine's baseline cut-offs (A)
+STATS = {"n128": (128, 0), "n4000": (4000, 1)}
 
 
-def gpu_means(mol):
-    p = engine.baseline_params()
+def engine_means(mol, runs, equil, every, samples):
+    """Per-run time averages of (rna_etot, Rg^2, Q, kinT) in the reference's
+    settings, one batched context, one Philox stream per run."""
+    p = engine.default_params(h=0.05, zeta=0.05, nnlup=50, nplup=1, seed=20240)
+    eps_e = np.full(len(mol.nat_i), 0.7, np.float32)   # coeff_att[1][1] (global.cpp:51-55)
     e = engine.Engine(p)
-    for k in range(SEEDS):
-        e.add(mol, mol.xyz, T=T, traj=k)
+    for k in range(runs):
+        e.add(mol, mol.xyz, T=T, traj=k, eps_energy=eps_e)
     e.commit()
-    e.step(EQUIL)
-    acc = np.zeros((SEEDS, 4))
-    for _ in range(SAMPLES):
-        e.step(EVERY)
-        for m in range(SEEDS):
+    e.step(equil)
+    acc = np.zeros((runs, 4))
+    for _ in range(samples):
+        e.step(every)
+        for m in range(runs):
             ob = e.observables(m)
             acc[m] += (e.energy(m)[4], ob["rgsq"], ob["Q"], ob["kinT"])
-        assert all(e.status(m)[0] == 0 for m in range(SEEDS))
+    failed = np.array([e.status(m)[0] != 0 for m in range(runs)])
     e.close()
-    return acc / SAMPLES
+    acc /= samples
+    acc[failed] = np.nan
+    return acc
 
 
-def ref_means(mol):
-    p = engine.baseline_params()
-
-    def one(k):
-        r = O.RefRun(mol, mol.xyz, CUT, 0.05, 0.05, T, 50, 10, 9000 + k, k)
-        r.advance(EQUIL)
-        acc = np.zeros(4)
-        for _ in range(SAMPLES):
-            r.advance(EVERY)
-            s = r.state()
-            x, v = s["unc_pos"], s["vel"]
-            nl_att, (nri, nrj), pl_att, (pri, prj) = oracle_lists(mol, x, p)
-            _, en = O.forces_f64(mol, x, pl_att, pri, prj)
-            ob = O.observables(mol, x, v)
-            acc += (en.sum(), ob["rgsq"], ob["Q"], ob["kinT"])
-        r.close()
-        return acc / SAMPLES
-
-    with ThreadPoolExecutor(16) as ex:
-        return np.array(list(ex.map(one, range(SEEDS))))
+@pytest.mark.parametrize("name", list(STATS))
+def test_long_runs_match_the_reference_program_within_2_sigma(name):
+    path = os.path.join(GOLD, "ref_stats.npz")
+    if not os.path.exists(path):
+        pytest.skip("ref_stats.npz not generated")
+    g = np.load(path)
+    ref = g[f"{name}.means"]
+    n, seed = STATS[name]
+    equil, every = int(g["equil"]), int(g["nup"])
+    samples = (int(g["nstep"]) - equil) // every
+    eng = engine_means(system.generate(n, seed), len(ref), equil, every, samples)
+    ok_e = np.isfinite(eng).all(1)
+    ok_r = np.isfinite(ref).all(1) & (ref[:, 3] < 10 * T)
+    fe, fr, nr = int((~ok_e).sum()), int((~ok_r).sum()), len(ref)
+    pool = (fe + fr) / (2.0 * nr)
+    print(name, "failed runs: engine", fe, "reference", fr, "of", nr)
+    assert abs(fe - fr) <= 3.0 * np.sqrt(2.0 * nr * pool * (1.0 - pool)) + 1.0, (fe, fr)
+    eng, ref = eng[ok_e], ref[ok_r]
+    zs = {}
+    for c, label in enumerate(("energy", "rgsq", "Q")):
+        se = np.sqrt(eng[:, c].var(ddof=1) / len(eng) + ref[:, c].var(ddof=1) / len(ref))
+        zs[label] = (eng[:, c].mean() - ref[:, c].mean()) / se
+    print(name, "z (engine - reference) / se:", {k: round(float(v), 2) for k, v in zs.items()},
+          "means engine", eng.mean(0).round(4), "reference", ref.mean(0).round(4))
+    for label, z in zs.items():
+        assert abs(z) <= 2.0, (name, label, z)
+    ke, kr = eng[:, 3].mean(), ref[:, 3].mean()
+    assert abs(ke - kr) < 0.01 * kr, (ke, kr)
 
 
 def test_same_noise_tracks_the_reference_loop():
@@ -96,21 +110,3 @@ def test_same_noise_tracks_the_reference_loop():
             assert dx < 1e-4 and dv < 1e-3, (traj, k, dx, dv)
         e.close()
         r.close()
-
-
-def test_long_run_statistics_match_reference_within_2_sigma():
-    mol = system.generate(128, 0)
-    g = gpu_means(mol)
-    r = ref_means(mol)
-    zs = {}
-    for c, name in enumerate(("energy", "rgsq", "Q")):
-        mg, mr = g[:, c].mean(), r[:, c].mean()
-        se = np.sqrt(g[:, c].var(ddof=1) / SEEDS + r[:, c].var(ddof=1) / SEEDS)
-        zs[name] = (mg - mr) / se
-    print("z (gpu - reference) / se:", {k: round(float(v), 2) for k, v in zs.items()})
-    for name, z in zs.items():
-        assert abs(z) <= 3.0, (name, z)
-    kg, kr = g[:, 3].mean(), r[:, 3].mean()
-    assert abs(kg - kr) < 0.01 * kr, (kg, kr)
-    # the comparison has power: the folded state is kept and T is reached
-    assert g[:, 2].mean() > 0.6 and abs(kg - T) < 0.03
