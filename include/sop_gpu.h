@@ -92,6 +92,13 @@ typedef struct sop_params {
                          there.  0 chosen by timing at commit, < 0 none, at
                          most 12288.  Served contexts use none.  Every window
                          gives the same bits. */
+  int step_buckets;   /* per-size-bucket tiles of a batched context: molecules
+                         of < 200, 200-599 and >= 600 beads each get the lanes
+                         per bead and the form the tuner chose for their
+                         bucket, in per-molecule tiles of one launch.  0: used
+                         when the tuner times it faster than the best
+                         whole-context step, 1: always (lanes and form must
+                         be left to the tuner), < 0: never.  Same bits. */
 } sop_params;
 
 /* Fills *p with the reference's defaults and the factor-mode list cut-offs. */
@@ -261,6 +268,13 @@ int sop_tuning(void* ctx, int* lanes, float* ms);
  * force kernel and a finish kernel, 3 persistent: the steps between two list
  * rebuilds in one launch). */
 int sop_step_form(void* ctx, int* lanes, int* form);
+
+/* The per-size-bucket tiling of the step (sop_params.step_buckets): *tiled
+ * receives 1 when the tiled step is in use; per bucket (< 200, 200-599,
+ * >= 600 beads) the lanes per bead and form chosen and the beads it holds
+ * (arrays of 3, NULL skips); ms[0], ms[1]: the tuned times of the tiled step
+ * and of the best whole-context step (0 when not tuned). */
+int sop_step_buckets(void* ctx, int* tiled, int* lanes, int* forms, long long* beads, float* ms);
 
 /* The step's shared-memory window in beads (0: partners gathered from global
  * memory). */

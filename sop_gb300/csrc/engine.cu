@@ -44,6 +44,8 @@ cudaError_t launch_step_persist(const DevSys& s, int G, int koff0, int count, bo
                                 unsigned* bar, unsigned long long limit_ns, cudaStream_t st);
 cudaError_t launch_barrier_check(const DevSys& s, int G, unsigned* bar, int missing, int rounds,
                                  unsigned long long limit_ns, cudaStream_t st);
+void launch_step_tiles(const DevSys& s, int koff, bool step, const int4* tiles, int ntiles,
+                       bool any_split, cudaStream_t st);
 void launch_advance(const DevSys& s, int steps, cudaStream_t st);
 void launch_gather_current(const DevSys& s, float* out, int* flag_out, cudaStream_t st);
 void launch_energy(const DevSys& s, int mol_start, int mol_n, int m, double* part, double* out,
@@ -194,6 +196,14 @@ struct SopCtx {
   bool split = false;         // step as force kernel + finish kernel
   int wcap = 0;               // > 0: step blocks stage their molecules (up to wcap beads)
   bool persist = false;       // steps between list rebuilds in one cooperative launch
+  // tiled form: per-molecule tiles, lanes and form chosen per size bucket
+  bool tiled = false;
+  int4* d_tiles = nullptr;    // {first bead, end bead, lanes, two-kernel form}
+  int ntiles = 0;
+  bool tiles_split = false;   // some bucket uses the two-kernel form (k_finish follows)
+  int bucket_lanes[3] = {0, 0, 0}, bucket_form[3] = {0, 0, 0};
+  long long bucket_beads[3] = {0, 0, 0};
+  float ms_tiled = 0.f, ms_whole = 0.f;  // tuning times of the two step layouts
   double* e_part = nullptr;   // energy / observable partials
   double* e_out = nullptr;    // 8 doubles
   double* h_out = nullptr;    // pinned copy of e_out
@@ -338,61 +348,25 @@ constexpr unsigned long long kBarrierLimitNs = 2000000000ull;
 
 unsigned* barrier_words(SopCtx* ctx) { return reinterpret_cast<unsigned*>(ctx->s.flags + 2); }
 
-// The largest bead window a step block would stage: the bead range from the
-// start of its first bead's molecule to the end of its last bead's, over
-// blocks of `bpb` beads (molecules are contiguous, packed ranges).
-int widest_window(const SopCtx* ctx, int bpb) {
-  std::vector<std::pair<int, int>> r;  // (start, n) by start
-  for (const HostMol& hm : ctx->mols)
-    if (hm.start >= 0 && hm.n > 0) r.emplace_back(hm.start, hm.n);
-  std::sort(r.begin(), r.end());
-  int widest = 0;
-  size_t m0 = 0, m1 = 0;
-  for (long long b0 = 0; b0 < ctx->s.nlive; b0 += bpb) {
-    const long long bl = std::min<long long>(b0 + bpb, ctx->s.nlive) - 1;
-    while (m0 + 1 < r.size() && r[m0 + 1].first <= b0) ++m0;
-    if (m1 < m0) m1 = m0;
-    while (m1 + 1 < r.size() && r[m1 + 1].first <= bl) ++m1;
-    if (m0 < r.size())
-      widest = std::max(widest, r[m1].first + r[m1].second - r[m0].first);
-  }
-  return widest;
-}
-
 // The step's window: sop_params.step_window > 0 fixes it, < 0 turns it off,
 // 0 lets the autotuner choose.
 int window_param(const SopCtx* ctx) { return ctx->P.step_window; }
 constexpr int kMaxStepWindow = 12288;  // 192 KB of shared memory per block
 constexpr int kMaxMolBeads = 65535;    // 16-bit molecule-relative pair-list partners
 
-// Picks the lanes per bead G, the form (one kernel or two) and the shared-
-// memory window of the step for this context by timing the force-only step
-// (idempotent: it recomputes the same forces and look-ahead from the same
-// state) for each candidate not fixed by the parameters; results are
-// bit-identical for every G, form and window, so only the speed differs.
-// Window candidates: none, and 1,024 / 2,048 beads (16 / 32 KB of shared
-// memory per block) where some block's molecules fit.
+// Picks the lanes per bead G and the form (one kernel or two) of the step
+// for this context by timing the force-only step (idempotent: it recomputes
+// the same forces and look-ahead from the same state) for each candidate not
+// fixed by the parameters; results are bit-identical for every G, form and
+// window, so only the speed differs.  A fixed window or the persistent form
+// (step_window > 0, step_split = 3) is timed as given.
 int autotune_lanes(SopCtx* ctx) {
   const int fixed_g = lanes_for(ctx), fixed_f = split_for(ctx), fixed_w = window_param(ctx);
   const int cand[4] = {2, 4, 8, 16};
-  std::vector<int> wins = {0};
-  if (!ctx->served && fixed_w > 0) {
-    wins = {fixed_w};
-  } else if (!ctx->served && fixed_w == 0) {
-    // widest window over blocks of 64 beads (the widest blocks, G = 2)
-    const int need = widest_window(ctx, 64);
-    bool small = false;
-    for (const HostMol& hm : ctx->mols) small |= hm.start >= 0 && hm.n > 0 && hm.n <= 2048;
-    if (small) {
-      if (need <= 2048) {
-        wins.push_back((need + 63) / 64 * 64);
-        if (need > 1024) wins.push_back(1024);
-      } else {
-        wins.push_back(1024);
-        wins.push_back(2048);
-      }
-    }
-  }
+  // the shared-memory window and the persistent form are measured slower
+  // than global gathers and per-step launches on every workload, so they are
+  // used where the parameters ask for them and not tried here
+  std::vector<int> wins = {(!ctx->served && fixed_w > 0) ? fixed_w : 0};
   // the opt-in is a per-kernel ceiling shared by every context of the
   // process: always the same (largest) value, so contexts never lower it
   // under one another; each launch asks for its own window only
@@ -408,7 +382,7 @@ int autotune_lanes(SopCtx* ctx) {
     if (fixed_g && g != fixed_g) continue;
     float gbest = 1e30f;
     for (int f = 1; f <= 3; ++f) {
-      if (fixed_f && f != fixed_f) continue;
+      if (fixed_f ? f != fixed_f : f == 3) continue;
       if (f == 3 && ctx->served) continue;
       const bool sp = f == 2;
       for (int wc : wins) {
@@ -507,6 +481,11 @@ void force_eval_async(SopCtx* ctx) {
 // among them): one persistent launch, or one launch per step.
 void launch_steps(SopCtx* ctx, int koff0, int count) {
   if (count <= 0) return;
+  if (ctx->tiled) {
+    for (int k = koff0; k < koff0 + count; ++k)
+      launch_step_tiles(ctx->s, k, true, ctx->d_tiles, ctx->ntiles, ctx->tiles_split, ctx->stream);
+    return;
+  }
   if (ctx->persist) {
     launch_step_persist(ctx->s, ctx->G, koff0, count, true, barrier_words(ctx), kBarrierLimitNs,
                         ctx->stream);
@@ -980,6 +959,107 @@ int uninstall(SopCtx* ctx, int slot) {
   return SOP_OK;
 }
 
+// Size buckets of the tiled form: molecules of fewer than 200 beads, of 200
+// to 599, and of 600 or more.
+constexpr int kBuckets = 3;
+int bucket_of(int n) { return n < 200 ? 0 : n < 600 ? 1 : 2; }
+
+// The tiles of every molecule (or of bucket `only` alone): runs of
+// 128 / lanes beads from the molecule's first bead, never across molecules.
+void build_tiles(const SopCtx* ctx, const int* lanes, const int* forms, int only,
+                 std::vector<int4>& out) {
+  out.clear();
+  for (const HostMol& hm : ctx->mols) {
+    if (hm.start < 0 || hm.n <= 0) continue;
+    const int b = bucket_of(hm.n);
+    if (only >= 0 && b != only) continue;
+    const int g = lanes[b], bpb = 128 / g;
+    for (int st = hm.start; st < hm.start + hm.n; st += bpb)
+      out.push_back(make_int4(st, std::min(st + bpb, hm.start + hm.n), g, forms[b] == 2));
+  }
+}
+
+// Times `reps` force-only evaluations of the current step layout (the tiles
+// in d_tiles when `tiles`, else the whole-context form); idempotent.
+int time_step(SopCtx* ctx, bool tiles, int ntiles, bool any_split, float* ms) {
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  auto run = [&] {
+    if (tiles) launch_step_tiles(ctx->s, 0, false, ctx->d_tiles, ntiles, any_split, ctx->stream);
+    else launch_step(ctx->s, ctx->G, ctx->split, 0, false, ctx->wcap, ctx->stream);
+  };
+  run();  // warm-up
+  CK(cudaEventRecord(a, ctx->stream));
+  for (int r = 0; r < 3; ++r) run();
+  CK(cudaEventRecord(b, ctx->stream));
+  CK(cudaEventSynchronize(b));
+  CK(cudaEventElapsedTime(ms, a, b));
+  *ms /= 3.0f;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  CK(cudaGetLastError());
+  return SOP_OK;
+}
+
+// The per-size-bucket tuner of a batched context: for each bucket, the lanes
+// per bead (4 or 8) and the form (one kernel or two) of its molecules' tiles,
+// timed on that bucket's tiles alone; then the tiled step with every
+// bucket's choice against the best whole-context form, and the faster one is
+// kept (sop_params.step_buckets 1 keeps the tiled step, -1 never tries it).
+// Both give the same bits.
+int autotune_buckets(SopCtx* ctx) {
+  const int want = ctx->P.step_buckets;
+  ctx->tiled = false;
+  if (want < 0 || ctx->served || ctx->persist || ctx->wcap > 0) return SOP_OK;
+  int present = 0;
+  for (int b = 0; b < kBuckets; ++b) ctx->bucket_beads[b] = 0;
+  long long cap = 0;
+  for (const HostMol& hm : ctx->mols)
+    if (hm.start >= 0 && hm.n > 0) {
+      ctx->bucket_beads[bucket_of(hm.n)] += hm.n;
+      cap += (hm.n + 15) / 16;
+    }
+  for (int b = 0; b < kBuckets; ++b) present += ctx->bucket_beads[b] > 0;
+  if (want == 0 && (present < 2 || ctx->mols.size() < 2)) return SOP_OK;
+  if (!ctx->d_tiles) {
+    ctx->d_tiles = ctx->dalloc<int4>((size_t)cap);
+    if (!ctx->d_tiles) return ctx->fail(SOP_ERR_ALLOC, "tile allocation failed");
+  }
+  std::vector<int4> t;
+  int lanes[kBuckets] = {4, 4, 4}, forms[kBuckets] = {1, 1, 1};
+  for (int b = 0; b < kBuckets; ++b) {
+    if (!ctx->bucket_beads[b]) continue;
+    float best = 1e30f;
+    for (int g : {4, 8})
+      for (int f : {1, 2}) {
+        int gl[kBuckets] = {g, g, g}, fl[kBuckets] = {f, f, f};
+        build_tiles(ctx, gl, fl, b, t);
+        CK(cudaMemcpy(ctx->d_tiles, t.data(), sizeof(int4) * t.size(), cudaMemcpyHostToDevice));
+        float ms = 0.f;
+        int rc = time_step(ctx, true, (int)t.size(), f == 2, &ms);
+        if (rc) return rc;
+        if (ms < best) { best = ms; lanes[b] = g; forms[b] = f; }
+      }
+  }
+  build_tiles(ctx, lanes, forms, -1, t);
+  CK(cudaMemcpy(ctx->d_tiles, t.data(), sizeof(int4) * t.size(), cudaMemcpyHostToDevice));
+  bool any_split = false;
+  for (int b = 0; b < kBuckets; ++b) any_split |= ctx->bucket_beads[b] && forms[b] == 2;
+  int rc = time_step(ctx, true, (int)t.size(), any_split, &ctx->ms_tiled);
+  if (rc) return rc;
+  rc = time_step(ctx, false, 0, false, &ctx->ms_whole);
+  if (rc) return rc;
+  for (int b = 0; b < kBuckets; ++b) {
+    ctx->bucket_lanes[b] = ctx->bucket_beads[b] ? lanes[b] : 0;
+    ctx->bucket_form[b] = ctx->bucket_beads[b] ? forms[b] : 0;
+  }
+  ctx->ntiles = (int)t.size();
+  ctx->tiles_split = any_split;
+  ctx->tiled = want > 0 || ctx->ms_tiled < ctx->ms_whole;
+  return SOP_OK;
+}
+
 // Set-up after installing molecules at step 0: lists from x_0, f_0 and the
 // look-ahead (sop.cu:142-186), and the lanes-per-bead choice.
 int setup_step0(SopCtx* ctx) {
@@ -999,9 +1079,15 @@ int setup_step0(SopCtx* ctx) {
   launch_pl_rebuild(ctx->s, -1, ctx->stream);
   force_eval_async(ctx);
   CK(cudaGetLastError());
-  if (!fixed_g || !fixed_f || (!fixed_w && !ctx->served)) {
+  if (!fixed_g || !fixed_f) {
     rc = autotune_lanes(ctx);
     if (rc) return rc;
+  }
+  if (!fixed_g && !fixed_f && !ctx->served) {
+    rc = autotune_buckets(ctx);
+    if (rc) return rc;
+  } else if (ctx->P.step_buckets > 0 && !ctx->served) {
+    return ctx->fail(SOP_ERR_ARG, "step_buckets = 1 needs the lanes and the form left to the tuner");
   }
   CK(cudaStreamSynchronize(ctx->stream));
   return SOP_OK;
@@ -1113,6 +1199,7 @@ void sop_params_default(sop_params* p) {
   p->integrator = 0;    // underdamped (param.cpp:249-253 selects)
   p->step_split = 0;    // autotuned
   p->step_window = 0;   // autotuned
+  p->step_buckets = 0;  // autotuned
 }
 
 int sop_ctx_create(const sop_params* p, void** out) {
@@ -2248,6 +2335,19 @@ int sop_check_step_barrier(void* p, int missing, double timeout_s, int* timed_ou
     CK(cudaMemsetAsync(ctx->s.flags, 0, 4 * sizeof(int), ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
   }
+  return SOP_OK;
+}
+
+int sop_step_buckets(void* p, int* tiled, int* lanes, int* forms, long long* beads, float* ms) {
+  if (!p) return SOP_ERR_ARG;
+  SopCtx* ctx = C(p);
+  if (tiled) *tiled = ctx->tiled ? 1 : 0;
+  for (int b = 0; b < kBuckets; ++b) {
+    if (lanes) lanes[b] = ctx->bucket_lanes[b];
+    if (forms) forms[b] = ctx->bucket_form[b];
+    if (beads) beads[b] = ctx->bucket_beads[b];
+  }
+  if (ms) { ms[0] = ctx->ms_tiled; ms[1] = ctx->ms_whole; }
   return SOP_OK;
 }
 

@@ -438,6 +438,55 @@ __global__ void __launch_bounds__(256, 6) k_finish(DevSys s, int koff) {
   finish_bead<STEP>(s, b, m, fs, koff);
 }
 
+// ------------------------------------------------------------ tiled form
+// Per-molecule tiles with per-tile shapes: each block takes one tile -- the
+// beads [t.x, t.y) of a single molecule (at most 128 / G of them) -- with
+// t.z lanes per bead (4 or 8) and t.w = 1 for the two-kernel form (the sum
+// goes to fsum for k_finish) or 0 (completed in the block).  The host builds
+// the tiles so that every molecule of a size bucket gets the shape the
+// autotuner chose for that bucket; one launch covers every bucket.  The
+// per-bead code is k_step's, so the bits are the same.
+template <int G, bool STEP, bool UNI>
+__device__ __forceinline__ void tile_body(const DevSys& s, int koff, int4 t, float4* fsum,
+                                          int* bead) {
+  constexpr int BPB = kStepThreads / G;
+  const int slot = threadIdx.x / G;
+  const int lane = threadIdx.x % G;
+  const int b1 = t.x + slot;
+  BeadSlot q;
+  if (b1 < t.y) q = bead_slot<STEP>(s, b1, koff);
+  float fx = 0.f, fy = 0.f, fz = 0.f;
+  bool fene_bad = false;
+  if (q.i >= 0)
+    bead_force<G, UNI>(s, GlobalX{s.x[(int)(q.n & 1)]}, q.i, q.m1, lane, q.br, q.ar, q.abase,
+                       q.acnt, q.rcnt, fx, fy, fz, fene_bad);
+  const float4 sum = marked_sum(fx, fy, fz, fene_bad, q.n);
+  if (t.w) {
+    if (q.i >= 0 && lane == 0) s.fsum[q.i] = sum;
+    return;
+  }
+  if (lane == 0) {
+    fsum[slot] = sum;
+    bead[slot] = q.i;
+  }
+  __syncthreads();
+  if (threadIdx.x >= BPB) return;
+  const int b = bead[threadIdx.x];
+  if (b >= 0) finish_bead<STEP>(s, b, s.mol_of[b], fsum[threadIdx.x], koff);
+}
+
+template <bool STEP, bool UNI>
+__global__ void __launch_bounds__(kStepThreads, StepBlocks<4>::value)
+    k_step_tiles(DevSys s, int koff, const int4* __restrict__ tiles) {
+  __shared__ float4 fsum[kStepThreads / 4];
+  __shared__ int bead[kStepThreads / 4];
+  pdl_wait();
+  pdl_release();
+  const int4 t = tiles[blockIdx.x];   // uniform over the block
+  if (t.z == 8) tile_body<8, STEP, UNI>(s, koff, t, fsum, bead);
+  else tile_body<4, STEP, UNI>(s, koff, t, fsum, bead);
+}
+
 // ------------------------------------------------------ persistent form
 // Every step of a run of steps with no list rebuild in between, in one
 // cooperative launch: each block owns bead chunks (grid-stride) and completes
@@ -515,7 +564,9 @@ __global__ void __launch_bounds__(kStepThreads, StepBlocks<G>::value)
   const int nchunks = (s.nlive + BPB - 1) / BPB;
   for (int k = 0; k < count; ++k) {
     if (k > 0 && !grid_barrier(bar, expected, gen, limit_ns, s.flags)) return;
-    const int koff = koff0 + k;
+    // steps advance the block offset; force-only evaluations (STEP = false,
+    // repeated for timing) recompute the same step, which keeps them idempotent
+    const int koff = STEP ? koff0 + k : koff0;
     for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
       const BeadSlot q = bead_slot<STEP>(s, c * BPB + slot, koff);
       float fx = 0.f, fy = 0.f, fz = 0.f;
@@ -772,6 +823,24 @@ void launch_step(const DevSys& s, int G, bool split, int koff, bool step, int wc
     case 4: launch_step_g<4>(s, split, koff, step, wcap, st); break;
     case 16: launch_step_g<16>(s, split, koff, step, wcap, st); break;
     default: launch_step_g<8>(s, split, koff, step, wcap, st); break;
+  }
+}
+
+// The tiled form: one launch over `ntiles` tiles, then k_finish when some
+// tile uses the two-kernel form.
+void launch_step_tiles(const DevSys& s, int koff, bool step, const int4* tiles, int ntiles,
+                       bool any_split, cudaStream_t st) {
+  if (ntiles <= 0) return;
+  if (s.uniform_type) {
+    if (step) launch_pdl(k_step_tiles<true, true>, (unsigned)ntiles, kStepThreads, st, s, koff, tiles);
+    else launch_pdl(k_step_tiles<false, true>, (unsigned)ntiles, kStepThreads, st, s, koff, tiles);
+  } else {
+    if (step) launch_pdl(k_step_tiles<true, false>, (unsigned)ntiles, kStepThreads, st, s, koff, tiles);
+    else launch_pdl(k_step_tiles<false, false>, (unsigned)ntiles, kStepThreads, st, s, koff, tiles);
+  }
+  if (any_split) {
+    if (step) launch_pdl(k_finish<true>, cdiv(s.nlive, 256), 256, st, s, koff);
+    else launch_pdl(k_finish<false>, cdiv(s.nlive, 256), 256, st, s, koff);
   }
 }
 

@@ -52,7 +52,7 @@ class Params(ctypes.Structure):
                 ("device", ctypes.c_int), ("graph_steps", ctypes.c_int),
                 ("lanes_per_bead", ctypes.c_int), ("seed", ctypes.c_ulonglong),
                 ("integrator", ctypes.c_int), ("step_split", ctypes.c_int),
-                ("step_window", ctypes.c_int)]
+                ("step_window", ctypes.c_int), ("step_buckets", ctypes.c_int)]
 
 
 class MoleculeDesc(ctypes.Structure):
@@ -143,6 +143,7 @@ def lib() -> ctypes.CDLL:
             "sop_serve_stats": (I, [V, V]),
             "sop_step_form": (I, [V, ctypes.POINTER(I), ctypes.POINTER(I)]),
             "sop_step_window": (I, [V, ctypes.POINTER(I)]),
+            "sop_step_buckets": (I, [V, ctypes.POINTER(I), V, V, V, V]),
             "sop_check_step_barrier": (I, [V, I, ctypes.c_double, ctypes.POINTER(I)]),
             "sop_checkpoint": (I, [V, I, V, LL, PLL]),
             "sop_restore": (I, [V, I, V, LL]),
@@ -374,7 +375,18 @@ class Engine:
         self._check(lib().sop_step_form(self.h, None, ctypes.byref(form)), self.h)
         win = ctypes.c_int()
         self._check(lib().sop_step_window(self.h, ctypes.byref(win)), self.h)
+        tiled = ctypes.c_int()
+        bl, bf = np.zeros(3, np.int32), np.zeros(3, np.int32)
+        bb, bms = np.zeros(3, np.int64), np.zeros(2, np.float32)
+        self._check(lib().sop_step_buckets(self.h, ctypes.byref(tiled), _p(bl), _p(bf), _p(bb),
+                                           _p(bms)), self.h)
+        buckets = {"tiled": bool(tiled.value), "ms_tiled": float(bms[0]),
+                   "ms_whole": float(bms[1]),
+                   "by_bucket": {name: {"beads": int(bb[k]), "lanes_per_bead": int(bl[k]),
+                                        "form": int(bf[k])}
+                                 for k, name in enumerate(("<200", "200-599", ">=600"))}}
         return {"lanes_per_bead": g.value, "form": form.value, "window": win.value,
+                "buckets": buckets,
                 "ms": {str(k): float(v) for k, v in zip((2, 4, 8, 16), ms)}}
 
     def check_step_barrier(self, missing: int, timeout_s: float) -> bool:

@@ -24,7 +24,8 @@ cannot run in the reference at these cut-offs: its repulsive pair list is
 empty and force_eval exits on the zero-block launch (energy.cu:92-110).
 
 Needs a GPU.  Run from the repository root:
-python tests/golden/make_ref_stats.py [--out PATH] [--jobs J]
+python tests/golden/make_ref_stats.py [--out PATH] [--jobs J] [--cases n128,n4000]
+    [--runs R --append]   (R more runs of the given cases, appended to PATH)
 """
 import argparse
 import os
@@ -95,21 +96,34 @@ def main() -> None:
     ap.add_argument("--out", default=os.path.join(HERE, "ref_stats.npz"))
     ap.add_argument("--jobs", type=int, default=min(12, os.cpu_count() or 4))
     ap.add_argument("--cases", default=",".join(STATS_CASES))
+    ap.add_argument("--runs", type=int, default=0, help="runs per case (0: the case's own count)")
+    ap.add_argument("--append", action="store_true",
+                    help="add the runs to those already in --out, with the next seeds")
     a = ap.parse_args()
     if not os.path.exists(EXE):
         sys.exit(f"{EXE} is missing: run bash oracle/build_ref.sh <reference tree>")
     out = {"T": np.float64(T), "nstep": np.int64(NSTEP), "nup": np.int64(NUP),
            "nnlup": np.int64(NNLUP), "equil": np.int64(EQUIL),
            "columns": np.array(["rna_etot", "rgsq", "Q", "kinT"])}
+    old = {}
+    if a.append and os.path.exists(a.out):
+        with np.load(a.out) as z:
+            old = {k: z[k] for k in z.files}
+        out.update(old)
     with tempfile.TemporaryDirectory() as work:
         for name in a.cases.split(","):
             c = STATS_CASES[name]
             mol = system.generate(c["n"], c["seed"])
             prefix = os.path.join(work, name)
             system.write_reference_files(mol, prefix)
-            seeds = [c["base"] + k * SEED_STRIDE for k in range(c["runs"])]
+            first = len(old.get(f"{name}.seeds", []))
+            runs = a.runs or c["runs"]
+            seeds = [c["base"] + k * SEED_STRIDE for k in range(first, first + runs)]
             with ThreadPoolExecutor(a.jobs) as ex:
                 means = list(ex.map(lambda s: run_one(prefix, s, work), seeds))
+            if first:
+                means = list(old[f"{name}.means"]) + means
+                seeds = list(old[f"{name}.seeds"]) + seeds
             out[f"{name}.means"] = np.array(means)
             out[f"{name}.seeds"] = np.array(seeds, np.int64)
             print(name, "mean over runs", np.array(means).mean(axis=0), flush=True)

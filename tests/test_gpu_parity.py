@@ -422,6 +422,32 @@ def test_step_window_bit_identical():
                 np.testing.assert_array_equal(o[k][key], outs[0][k][key])
 
 
+def test_size_bucket_tiles_bit_identical():
+    """The per-size-bucket tiled step (each molecule in tiles of its bucket's
+    lanes and form, one launch) gives the bits of the whole-context step: a
+    batched context with molecules in all three buckets, tiled forced on and
+    off; the tuner reports a choice for every bucket."""
+    mols = [mol_of(n, 60 + k) for k, n in enumerate((70, 150, 330, 520, 900, 1400, 45))]
+    outs = []
+    for buckets in (1, -1):
+        e = engine.Engine(engine.baseline_params(step_buckets=buckets))
+        for k, m in enumerate(mols):
+            e.add(m, m.xyz, T=0.6, traj=k)
+        e.commit()
+        t = e.tuning()["buckets"]
+        assert t["tiled"] == (buckets == 1)
+        if buckets == 1:
+            for name, b in t["by_bucket"].items():
+                assert b["beads"] > 0 and b["lanes_per_bead"] in (4, 8) and b["form"] in (1, 2)
+            assert t["ms_tiled"] > 0 and t["ms_whole"] > 0
+        e.step(60)
+        outs.append([e.download(k) for k in range(len(mols))])
+        e.close()
+    for k in range(len(mols)):
+        for key in ("unc_pos", "vel", "force"):
+            np.testing.assert_array_equal(outs[0][k][key], outs[1][k][key])
+
+
 def test_persistent_step_barrier_wait_ends():
     """The persistent form's device-wide barrier completes when every block
     arrives, and when an arrival never comes its wait runs out after the
