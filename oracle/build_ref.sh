@@ -10,6 +10,9 @@
 #                     cuRAND noise; needs a GPU
 #   sop2ref.x         the reference program itself (main() of sop.cu) over the
 #                     same objects as libsopref_gpu.so
+#   sop2ref_hostrng.x the same program built with its host noise generator
+#                     instead of cuRAND (USE_CURAND taken back, through
+#                     ref_energy_hostrng.cu and ref_sop_hostrng.cu)
 #
 # Every artefact links with the wrappers of ref_link_wraps.cpp (host-side
 # copies for the host filters, an optional cuRAND seed from the environment).
@@ -46,6 +49,8 @@ for src in energy.cu GPUvars.cu sop.cu; do
   "$NVCC" "${flags[@]}" -c "$ref/$src" -o "$o/${src%.cu}.o" & pids+=($!)
 done
 "$NVCC" "${flags[@]}" -c "$here/ref_sop_cpu_lists.cu" -o "$o/sop_cpu_lists.o" & pids+=($!)
+"$NVCC" "${flags[@]}" -c "$here/ref_energy_hostrng.cu" -o "$o/energy_hostrng.o" & pids+=($!)
+"$NVCC" "${flags[@]}" -c "$here/ref_sop_hostrng.cu" -o "$o/sop_hostrng.o" & pids+=($!)
 "$NVCC" "${flags[@]}" -x cu -c "$here/ref_harness.cpp" -o "$o/ref_harness.o" & pids+=($!)
 "$NVCC" -std=c++17 "${base[@]}" -c "$here/ref_cudpp_cub.cu" -o "$o/ref_cudpp_cub.o" & pids+=($!)
 "$NVCC" "${flags[@]}" -x cu -c "$here/ref_link_wraps.cpp" -o "$o/ref_link_wraps.o" & pids+=($!)
@@ -62,5 +67,9 @@ shared=(-shared -Xlinker -Bsymbolic)
 "$NVCC" "${shared[@]}" "${arch[@]}" "${wraps[@]}" -o "$out/libsopref_gpu.so" \
   "${common[@]}" "$o/sop.o" "$o/ref_harness.o" & l2=$!
 "$NVCC" "${arch[@]}" "${wraps[@]}" -o "$out/sop2ref.x" "${common[@]}" "$o/sop.o" & l3=$!
-wait $l1; wait $l2; wait $l3
-echo "build_ref: $out/libsopref.so $out/libsopref_gpu.so $out/sop2ref.x (from $ref)"
+hostrng=()
+for f in "${common[@]}"; do [ "$f" = "$o/energy.o" ] || hostrng+=("$f"); done
+"$NVCC" "${arch[@]}" "${wraps[@]}" -o "$out/sop2ref_hostrng.x" "${hostrng[@]}" \
+  "$o/energy_hostrng.o" "$o/sop_hostrng.o" & l4=$!
+wait $l1; wait $l2; wait $l3; wait $l4
+echo "build_ref: $out/libsopref.so $out/libsopref_gpu.so $out/sop2ref.x $out/sop2ref_hostrng.x (from $ref)"

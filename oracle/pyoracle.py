@@ -46,6 +46,8 @@ def lib() -> ctypes.CDLL:
         L.orc_filter_rep.restype = ctypes.c_longlong
         L.orc_rcut2.restype = ctypes.c_float
         L.orc_rcut2.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_float]
+        L.orc_ref_rgsq.restype = ctypes.c_double
+        L.orc_ref_rgsq.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_double]
         _LIB = L
     return _LIB
 
@@ -135,6 +137,23 @@ def noise_normals(n, step, traj, seed):
     lib().orc_noise_normals(n, ctypes.c_ulonglong(step), ctypes.c_uint(traj),
                             ctypes.c_ulonglong(seed), _p(out))
     return out
+
+
+def ref_gasdev(run_id: int, count: int) -> np.ndarray:
+    """The reference's host Gaussian deviates after `set run` = run_id
+    (random_generator.cpp:83-143, restated in orc_ref_gasdev)."""
+    out = np.empty(count, np.float64)
+    lib().orc_ref_gasdev(int(run_id), ctypes.c_longlong(count), _p(out))
+    return out
+
+
+def ref_rgsq(unc: np.ndarray, boxl: float) -> float:
+    """Rg^2 of unwrapped coordinates as the reference computes it: the float
+    pair sum of calculate_observables (sop.cu:563-580), restated in
+    orc_ref_rgsq.  Thread-safe (ctypes releases the GIL), so a pool of
+    threads can measure many frames at once."""
+    x = np.ascontiguousarray(unc, np.float32)
+    return lib().orc_ref_rgsq(int(x.shape[0]), x.ctypes.data, float(boxl))
 
 
 def langevin_consts(h, zeta, T):

@@ -581,3 +581,108 @@ void orc_ref_state(const orc_ref* r, float* unc, float* pos, float* vel) {
   if (pos) memcpy(pos, r->pos, f3);
   if (vel) memcpy(vel, r->vel, f3);
 }
+
+/* ------------------------------------------------------------------------
+ * The reference's host Gaussian generator (random_generator.cpp:83-143): the
+ * L'Ecuyer two-stream generator with a Bays-Durham shuffle ("ran2" of
+ * Numerical Recipes, 2nd ed., section 7.1) and the polar Box-Muller method
+ * ("gasdev", section 7.2), in the reference's types: FLOAT (float) results,
+ * the constant expressions in double.  Seeded as `set run N` seeds it
+ * (param.cpp:274-279: seed -100 - N).  With it the reference program built
+ * without USE_CURAND draws var * gasdev() per bead and component, bead by
+ * bead, x y z, at every force evaluation (energy.cu:168-188).
+ */
+typedef struct {
+  int mseed, iset, idum2, iy, iv[32];
+  float gset;
+} orc_rangen;
+
+static float rangen_ran2(orc_rangen* g) {
+  const int IM1 = 2147483563, IM2 = 2147483399, IA1 = 40014, IA2 = 40692, IQ1 = 53668,
+            IQ2 = 52774, IR1 = 12211, IR2 = 3791, NTAB = 32, IMM1 = IM1 - 1,
+            NDIV = 1 + IMM1 / NTAB;
+  const float AM = (float)(1.0 / (float)2147483563), RNMX = (float)(1.0 - 3.0e-16);
+  int j, k;
+  float temp;
+  if (g->mseed <= 0) {
+    g->mseed = (g->mseed == 0 ? 1 : -g->mseed);
+    g->idum2 = g->mseed;
+    for (j = NTAB + 7; j >= 0; j--) {
+      k = g->mseed / IQ1;
+      g->mseed = IA1 * (g->mseed - k * IQ1) - k * IR1;
+      if (g->mseed < 0) g->mseed += IM1;
+      if (j < NTAB) g->iv[j] = g->mseed;
+    }
+    g->iy = g->iv[0];
+  }
+  k = g->mseed / IQ1;
+  g->mseed = IA1 * (g->mseed - k * IQ1) - k * IR1;
+  if (g->mseed < 0) g->mseed += IM1;
+  k = g->idum2 / IQ2;
+  g->idum2 = IA2 * (g->idum2 - k * IQ2) - k * IR2;
+  if (g->idum2 < 0) g->idum2 += IM2;
+  j = g->iy / NDIV;
+  g->iy = g->iv[j] - g->idum2;
+  g->iv[j] = g->mseed;
+  if (g->iy < 1) g->iy += IMM1;
+  temp = AM * g->iy;
+  return temp > RNMX ? RNMX : temp;
+}
+
+static float rangen_gasdev(orc_rangen* g) {
+  float fac, rsq, v1, v2;
+  if (g->iset == 0) {
+    do {
+      v1 = (float)(2.0 * rangen_ran2(g) - 1.0);
+      v2 = (float)(2.0 * rangen_ran2(g) - 1.0);
+      rsq = v1 * v1 + v2 * v2;
+    } while (rsq >= 1.0 || rsq == 0.0);
+    /* the reference is C++ with `using namespace std`: log of a float is
+       the float overload, the rest of the expression double */
+    fac = (float)sqrt(-2.0 * logf(rsq) / rsq);
+    g->gset = v1 * fac;
+    g->iset = 1;
+    return v2 * fac;
+  }
+  g->iset = 0;
+  return g->gset;
+}
+
+/* `count` deviates of the generator after `set run` = run_id, from its
+ * start (a fresh generator: iset 0, idum2 123456789, iy 0). */
+void orc_ref_gasdev(int run_id, long long count, double* out) {
+  orc_rangen g;
+  memset(&g, 0, sizeof g);
+  g.idum2 = 123456789;
+  g.mseed = -100 - run_id;
+  for (long long k = 0; k < count; ++k) out[k] = rangen_gasdev(&g);
+}
+
+/* ------------------------------------------------------------------------
+ * Rg^2 as the reference computes it (calculate_observables, sop.cu:563-580):
+ * every pair i < j in loop order, the minimum image with the host rnd()
+ * (misc.cpp:4-11, half away from zero), and the sum of squared distances
+ * accumulated in FLOAT (float), then divided by N^2.  For thousands of beads
+ * the float sum of millions of positive terms loses low bits at every
+ * addition, and the result falls below the exact value (-0.4% for 4,000
+ * beads); this restatement reproduces that value bit for bit, so an engine
+ * trajectory can be measured with the reference's own estimator.
+ */
+static float ref_rnd(float x) { return (float)((x > 0) ? floor(x + 0.5) : ceil(x - 0.5)); }
+
+double orc_ref_rgsq(int n, const float* x, double boxl_d) {
+  const float boxl = (float)boxl_d;
+  float rg = 0.0f;
+  for (int i = 0; i < n - 1; ++i)
+    for (int j = i + 1; j < n; ++j) {
+      float dx = x[3 * i] - x[3 * j];
+      float dy = x[3 * i + 1] - x[3 * j + 1];
+      float dz = x[3 * i + 2] - x[3 * j + 2];
+      dx -= boxl * ref_rnd(dx / boxl);
+      dy -= boxl * ref_rnd(dy / boxl);
+      dz -= boxl * ref_rnd(dz / boxl);
+      rg += (dx * dx + dy * dy + dz * dz);
+    }
+  rg /= (float)(n * n);
+  return rg;
+}

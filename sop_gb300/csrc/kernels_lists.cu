@@ -357,8 +357,7 @@ __device__ __forceinline__ float slab_dist(float v, float a, float w) {
 // d^2 < (fac*sigma or abs)^2 in FP32, |i - j| > 2, not a native contact) are
 // written to the bead's fixed-stride row in candidate order (group ballot).
 // The culling is conservative (a 1e-3 A margin); membership is decided by the
-// exact predicate alone.  The bead's native partners sit in registers, with
-// a 64-bit filter of their indices in front of the compares.
+// exact predicate alone.  The bead's native partners sit in registers.
 template <bool UNI>
 __global__ void __launch_bounds__(256) k_nl(DevSys s) {
   const int k = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) / kNlLanes);
@@ -389,13 +388,6 @@ __global__ void __launch_bounds__(256) k_nl(DevSys s) {
   int nat[kNatRegs];
 #pragma unroll
   for (int q = 0; q < kNatRegs; ++q) nat[q] = q < nrow.y ? s.nat_j[nrow.x + q] : -1;
-  // a 64-bit filter of the native partners (bit j & 63): a candidate whose
-  // bit is clear is no native partner, so most candidates skip the compares
-  unsigned long long nfilter = 0ull;
-#pragma unroll
-  for (int q = 0; q < kNatRegs; ++q)
-    if (nat[q] >= 0) nfilter |= 1ull << (nat[q] & 63);
-  for (int q = kNatRegs; q < nrow.y; ++q) nfilter |= 1ull << (s.nat_j[nrow.x + q] & 63);
   const long long stride = s.nl_stride;
   int* row = s.nl_j + (long long)i * stride;
   int cnt = 0;
@@ -431,7 +423,7 @@ __global__ void __launch_bounds__(256) k_nl(DevSys s) {
                   dz2 = __fsub_rn(xj.z, xi.z);
             if (wrap) min_image3(dx, dy2, dz2, boxl);
             pass = d2_exact(dx, dy2, dz2) < (UNI ? r11 : pick_type_pair(r11, r12, r22, ti, wj & 3));
-            if (pass && ((nfilter >> (j & 63)) & 1ull)) {
+            if (pass) {
               bool native = false;
 #pragma unroll
               for (int q = 0; q < kNatRegs; ++q) native |= (nat[q] == j);

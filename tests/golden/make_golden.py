@@ -23,12 +23,18 @@ Fixtures:
                                the reference's output writers (io.cpp:261-381)
                                on that state (wrapped = unwrapped coordinates)
   m128_update.txt              its progress line for step 1000 (sop.cu:256-259)
+  ref_gasdev.npz               the first 3,000 deviates of the reference's host
+                               Gaussian generator (random_generator.cpp:83-143)
+                               after `set run 7` and `set run 0`
   ref_lists.npz                the reference's host-filter neighbour and pair
                                lists (factor mode, sop.cu:1351-1448, 1707-1823)
                                for every structure of cases.py: sorted pair
                                keys for the 128-bead cases, SHA-256 digests of
                                the sorted keys and the counts for the
                                4,000-bead ones
+  ref_rgsq.npz                 the reference's Rg^2 (calculate_observables,
+                               sop.cu:563-580, float accumulation) on every
+                               structure of cases.py
 
 Run from the repository root: python tests/golden/make_golden.py
 """
@@ -141,17 +147,29 @@ def main():
     np.savez_compressed(os.path.join(HERE, "m128_energy.npz"), x=x, v=v, observables=ob,
                         coeff_att_11=np.float32(0.7), **fx)
     reference_case_lists(R)
+    dev = {}
+    for run in (7, 0):
+        g = np.zeros(3000)
+        R.ref_gasdev(run, 3000, P(g))
+        dev[f"run{run}"] = g
+    np.savez_compressed(os.path.join(HERE, "ref_gasdev.npz"), **dev)
     print("golden fixtures written to", HERE)
 
 
 def reference_case_lists(R):
-    """ref_lists.npz: the reference's host filters on every case."""
+    """ref_lists.npz and ref_rgsq.npz: the reference's host filters and its
+    Rg^2 on every case."""
     import tempfile
-    out = {}
+    out, rg = {}, {}
     with tempfile.TemporaryDirectory() as d:
         for name in cases.CASES:
             mol, x, _, boxl = cases.build(name)
             O.ref_load_molecule(R, mol, x, boxl, os.path.join(d, name))
+            x32 = np.ascontiguousarray(x, np.float32)
+            R.ref_set_state(P(x32), None)
+            ob = np.zeros(4)
+            R.ref_observables(P(ob))
+            rg[name] = np.float64(ob[1])
             R.ref_host_lists_prepare()
             lists = O.ref_lists(R)
             for which, (i, j, _) in lists.items():
@@ -163,6 +181,7 @@ def reference_case_lists(R):
                     out[f"{name}.{which}.sha256"] = np.array(cases.digest(keys))
             print(name, {k: len(v[0]) for k, v in lists.items()})
     np.savez_compressed(os.path.join(HERE, "ref_lists.npz"), **out)
+    np.savez_compressed(os.path.join(HERE, "ref_rgsq.npz"), **rg)
 
 
 if __name__ == "__main__":

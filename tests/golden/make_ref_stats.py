@@ -5,7 +5,7 @@ The reference program itself (oracle/_ref/sop2ref.x: main() and
 underdamped_ctrl of sop.cu, built by oracle/build_ref.sh) runs its own input
 script on each structure once per seed:
 
-  set dynamics underdamped; set temp T; set zeta 0.05; set t_step 0.05;
+  set run R; set dynamics underdamped; set temp T; set zeta 0.05; set t_step 0.05;
   set nstep 5000; set nup 100; set nnlup 50; set cutofftype neighborlist;
   set boxl 500; load bonds|angles|vdw|init <files>; run;
 
@@ -18,8 +18,9 @@ nup steps (sop.cu:252-262) gives, after EQUIL steps, SAMPLES rows per run:
 rna_etot (its native energy uses coeff_att, 0.7 for type (1, 1)), Rg^2, Q and
 the kinetic temperature.  Their per-run means are stored, one row per seed.
 
-Cases: the 128-bead structure (seed 0) and the 4,000-bead structure (seed
-1), both from the native structure at kBT = 0.6.  A fully extended start
+Cases: the 128-bead structure (seed 0, 256 runs) and the 4,000-bead
+structure (seed 1, 144 runs: 48, then 96 more with --append), both from the
+native structure at kBT = 0.6.  A fully extended start
 cannot run in the reference at these cut-offs: its repulsive pair list is
 empty and force_eval exits on the zero-block launch (energy.cu:92-110).
 
@@ -43,6 +44,9 @@ sys.path.insert(0, ROOT)
 from sop_gb300 import system  # noqa: E402
 
 EXE = os.path.join(ROOT, "oracle", "_ref", "sop2ref.x")
+# the same program built with its host noise generator (--rng host):
+# gasdev of random_generator.cpp seeded by `set run`, in place of cuRAND
+EXE_HOST = os.path.join(ROOT, "oracle", "_ref", "sop2ref_hostrng.x")
 T = 0.6
 NSTEP, NUP, NNLUP, EQUIL = 5000, 100, 50, 1000
 # setup_rng seeds bead i's XORWOW generator with seed + i (GPUvars.cu:417-425);
@@ -52,7 +56,8 @@ STATS_CASES = {"n128": dict(n=128, seed=0, runs=256, base=1_000_000),
                "n4000": dict(n=4000, seed=1, runs=48, base=900_000_000)}
 
 
-SCRIPT = """set dynamics underdamped;
+SCRIPT = """set run {run};
+set dynamics underdamped;
 set temp {T};
 set zeta 0.05;
 set t_step 0.05;
@@ -69,12 +74,15 @@ run;
 """
 
 
-def run_one(prefix: str, seed: int, workroot: str) -> np.ndarray:
+def run_one(prefix: str, seed: int, workroot: str, exe: str = EXE) -> np.ndarray:
     d = tempfile.mkdtemp(dir=workroot)
     with open(os.path.join(d, "input"), "w") as f:
-        f.write(SCRIPT.format(T=T, nstep=NSTEP, nup=NUP, nnlup=NNLUP, p=prefix))
+        # `set run` seeds the host generator (param.cpp:274-279): runs stay
+        # distinct whichever noise path the program was built with
+        f.write(SCRIPT.format(T=T, nstep=NSTEP, nup=NUP, nnlup=NNLUP, p=prefix,
+                              run=seed % 1_000_000_007))
     env = dict(os.environ, SOP_REF_CURAND_SEED=str(seed))
-    subprocess.run([EXE, "input"], cwd=d, env=env, check=True, stdout=subprocess.DEVNULL,
+    subprocess.run([exe, "input"], cwd=d, env=env, check=True, stdout=subprocess.DEVNULL,
                    stderr=subprocess.DEVNULL)
     rows = []
     with open(os.path.join(d, "update.out")) as f:
@@ -99,9 +107,12 @@ def main() -> None:
     ap.add_argument("--runs", type=int, default=0, help="runs per case (0: the case's own count)")
     ap.add_argument("--append", action="store_true",
                     help="add the runs to those already in --out, with the next seeds")
+    ap.add_argument("--rng", choices=["curand", "host"], default="curand",
+                    help="noise path of the reference program (host: its gasdev generator)")
     a = ap.parse_args()
-    if not os.path.exists(EXE):
-        sys.exit(f"{EXE} is missing: run bash oracle/build_ref.sh <reference tree>")
+    exe = EXE if a.rng == "curand" else EXE_HOST
+    if not os.path.exists(exe):
+        sys.exit(f"{exe} is missing: run bash oracle/build_ref.sh <reference tree>")
     out = {"T": np.float64(T), "nstep": np.int64(NSTEP), "nup": np.int64(NUP),
            "nnlup": np.int64(NNLUP), "equil": np.int64(EQUIL),
            "columns": np.array(["rna_etot", "rgsq", "Q", "kinT"])}
@@ -120,7 +131,7 @@ def main() -> None:
             runs = a.runs or c["runs"]
             seeds = [c["base"] + k * SEED_STRIDE for k in range(first, first + runs)]
             with ThreadPoolExecutor(a.jobs) as ex:
-                means = list(ex.map(lambda s: run_one(prefix, s, work), seeds))
+                means = list(ex.map(lambda s: run_one(prefix, s, work, exe), seeds))
             if first:
                 means = list(old[f"{name}.means"]) + means
                 seeds = list(old[f"{name}.seeds"]) + seeds

@@ -222,3 +222,23 @@ def test_output_writers_match_reference_writers(tmp_path):
     line = outputs.update_line(1000, 0.6, kinT, [e[0], e[1], e[2], e[3], 0.0], Q, int(contct), rgsq)
     with open(os.path.join(GOLD, "m128_update.txt")) as f:
         assert line == f.read().strip()
+
+
+def test_oracle_gasdev_is_the_reference_generator():
+    """The oracle's restatement of the reference's host Gaussian generator
+    (ran2 + polar Box-Muller in the reference's float types) reproduces the
+    reference's own deviates bit for bit."""
+    g = np.load(os.path.join(GOLD, "ref_gasdev.npz"))
+    for run in (7, 0):
+        np.testing.assert_array_equal(O.ref_gasdev(run, 3000), g[f"run{run}"])
+
+
+def test_oracle_rgsq_is_the_reference_estimator():
+    """The oracle's restatement of the reference's Rg^2 (a float sum over all
+    pairs, sop.cu:563-580) gives the reference's own values bit for bit on
+    every structure of cases.py, 4,000 beads included, where the float sum
+    already sits 0.4% below the exact one."""
+    ref = np.load(os.path.join(GOLD, "ref_rgsq.npz"))
+    for name in cases.CASES:
+        mol, x, _, boxl = cases.build(name)
+        assert O.ref_rgsq(x, boxl) == float(ref[name]), name
