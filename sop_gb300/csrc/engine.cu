@@ -309,23 +309,17 @@ int grow_nl_keep(SopCtx* ctx, long long stride);
 
 namespace {
 
-// The rows of beads o .. o + n - 1 of the repulsive neighbour list (r = 0,
-// absolute bead indices) or pair list (r = 1, molecule-relative), every
-// entry as an index relative to bead o, full row stride.
+// The rows of the molecule whose beads are o .. o + n - 1 in the repulsive
+// neighbour list (r = 0) or pair list (r = 1), every entry as an index
+// relative to bead o (as stored), full row stride.
 int read_rows(SopCtx* ctx, int r, int o, int n, std::vector<int>& rows) {
   const long long stride = ctx->s.nl_stride, len = stride * n;
   rows.assign((size_t)len, 0);
   if (!len) return SOP_OK;
-  if (r == 0) {
-    CK(cudaMemcpy(rows.data(), ctx->s.nl_j + (long long)o * stride, sizeof(int) * len,
-                  cudaMemcpyDeviceToHost));
-    for (auto& v : rows) v -= o;
-  } else {
-    std::vector<unsigned short> h((size_t)len);
-    CK(cudaMemcpy(h.data(), ctx->s.pl_j + (long long)o * stride, sizeof(unsigned short) * len,
-                  cudaMemcpyDeviceToHost));
-    for (size_t k = 0; k < h.size(); ++k) rows[k] = h[k];
-  }
+  std::vector<unsigned short> h((size_t)len);
+  CK(cudaMemcpy(h.data(), (r == 0 ? ctx->s.nl_j : ctx->s.pl_j) + (long long)o * stride,
+                sizeof(unsigned short) * len, cudaMemcpyDeviceToHost));
+  for (size_t k = 0; k < h.size(); ++k) rows[k] = h[k];
   return SOP_OK;
 }
 
@@ -424,14 +418,14 @@ int autotune_lanes(SopCtx* ctx) {
 
 // (Re)allocates the fixed-stride neighbour / pair-list rows.
 int alloc_nl(SopCtx* ctx, long long stride) {
-  stride = (stride + 31) / 32 * 32;  // rows stay 16-byte aligned
+  stride = (stride + 31) / 32 * 32;  // rows stay 64-byte aligned
   const long long entries = stride * (long long)ctx->s.nbead;
   // rows are addressed with 64-bit offsets; the bound only keeps the byte
-  // count (two int arrays) far from overflow
+  // count (two arrays of 16-bit entries) far from overflow
   if (entries > (1LL << 40)) return ctx->fail(SOP_ERR_CAPACITY, "neighbour list exceeds 2^40 entries");
   ctx->dfree(ctx->s.nl_j);
   ctx->dfree(ctx->s.pl_j);
-  ctx->s.nl_j = ctx->dalloc<int>(entries);
+  ctx->s.nl_j = ctx->dalloc<unsigned short>(entries);
   ctx->s.pl_j = ctx->dalloc<unsigned short>(entries);
   if (!ctx->s.nl_j || !ctx->s.pl_j) return ctx->fail(SOP_ERR_ALLOC, "neighbour-list allocation failed");
   ctx->s.nl_stride = stride;
@@ -1358,14 +1352,14 @@ int grow_nl_keep(SopCtx* ctx, long long stride) {
   if (stride <= s.nl_stride) return SOP_OK;
   const long long nb = s.nbead, old = s.nl_stride, entries = stride * nb;
   if (entries > (1LL << 40)) return ctx->fail(SOP_ERR_CAPACITY, "neighbour list exceeds 2^40 entries");
-  int* nj = ctx->dalloc<int>(entries);
+  unsigned short* nj = ctx->dalloc<unsigned short>(entries);
   unsigned short* pj = ctx->dalloc<unsigned short>(entries);
   if (!nj || !pj) {
     ctx->dfree(nj);
     ctx->dfree(pj);
     return ctx->fail(SOP_ERR_ALLOC, "neighbour-list allocation failed");
   }
-  CK(cudaMemcpy2D(nj, 4 * stride, s.nl_j, 4 * old, 4 * old, nb, cudaMemcpyDeviceToDevice));
+  CK(cudaMemcpy2D(nj, 2 * stride, s.nl_j, 2 * old, 2 * old, nb, cudaMemcpyDeviceToDevice));
   CK(cudaMemcpy2D(pj, 2 * stride, s.pl_j, 2 * old, 2 * old, nb, cudaMemcpyDeviceToDevice));
   ctx->dfree(s.nl_j);
   ctx->dfree(s.pl_j);
@@ -1507,15 +1501,15 @@ int restore_into(SopCtx* ctx, int slot, const char* buf, long long len) {
     if (rc) return rc;
   }
   const long long stride = s.nl_stride;
-  std::vector<int> rows[2];
+  std::vector<unsigned short> rows[2];   // both molecule-relative, as stored
   for (int k = 0; k < 2; ++k) {
-    rows[k].assign((size_t)(stride * n), k == 0 ? o : 0);
+    rows[k].assign((size_t)(stride * n), 0);
     for (int i = 0; i < n; ++i)
       for (int t = 0; t < cnt[(size_t)(2 + k) * n + i]; ++t) {
         int v;
         get(&v, sizeof v);
         if (v < 0 || v >= n) return ctx->fail(SOP_ERR_ARG, "corrupt checkpoint");
-        rows[k][(size_t)i * stride + t] = k == 0 ? v + o : v;
+        rows[k][(size_t)i * stride + t] = (unsigned short)v;
       }
   }
   const int cur = (int)(h.step & 1);
@@ -1530,11 +1524,10 @@ int restore_into(SopCtx* ctx, int slot, const char* buf, long long len) {
     CK(cudaMemcpy(s.nl_att_e + hm.off_n, ae.data(), sizeof(int) * nn2, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(s.pl_att + hm.off_n, ap.data(), sizeof(float4) * nn2, cudaMemcpyHostToDevice));
   }
-  CK(cudaMemcpy(s.nl_j + (long long)o * stride, rows[0].data(), sizeof(int) * rows[0].size(),
-                cudaMemcpyHostToDevice));
-  std::vector<unsigned short> prow(rows[1].begin(), rows[1].end());
-  CK(cudaMemcpy(s.pl_j + (long long)o * stride, prow.data(), sizeof(unsigned short) * prow.size(),
-                cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s.nl_j + (long long)o * stride, rows[0].data(),
+                sizeof(unsigned short) * rows[0].size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s.pl_j + (long long)o * stride, rows[1].data(),
+                sizeof(unsigned short) * rows[1].size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s.mol_step + slot, &h.step, sizeof(long long), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(s.mol_status + slot, &h.status, sizeof(int), cudaMemcpyHostToDevice));
   return SOP_OK;
@@ -1666,7 +1659,8 @@ int sop_serve_create(const sop_params* p, long long budget_bytes, long long max_
   stride = std::max<long long>(64, (stride + 31) / 32 * 32);
   // bytes per bead slot: state (8 float4), counters and cell data (10 ints),
   // rows (3 int2), topology (2 bond, 2 angle, 8 native entries) and list rows
-  const long long per_bead = 128 + 40 + 24 + 16 + 8 + 8 * 48 + 8 * stride;
+  // (neighbour and pair list, 16-bit entries)
+  const long long per_bead = 128 + 40 + 24 + 16 + 8 + 8 * 48 + 4 * stride;
   Caps c;
   c.beads = std::max<long long>(max_job_beads, budget_bytes / per_bead);
   c.mols = std::max<long long>(64, c.beads / 50);
@@ -2289,7 +2283,7 @@ int sop_memory(void* p, int mol, long long* ctx_bytes, long long* mol_bytes) {
     if (mol < 0 || mol >= (int)ctx->mols.size()) return ctx->fail(SOP_ERR_NOT_FOUND, "unknown molecule");
     const HostMol& hm = ctx->mols[mol];
     long long per_bead = 7 * 16 + 4 * 10 + 16 + 3 * 8;
-    long long nl = ctx->s.nl_stride * 8LL * hm.n;
+    long long nl = ctx->s.nl_stride * 4LL * hm.n;   // two rows of 16-bit entries
     *mol_bytes = per_bead * hm.n + nl + (long long)(hm.bi.size() + hm.ai.size()) * 16 +
                  (long long)hm.ni.size() * 2 * 40;
   }

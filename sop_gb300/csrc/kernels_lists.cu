@@ -358,8 +358,9 @@ __device__ __forceinline__ float slab_dist(float v, float a, float w) {
 // written to the bead's fixed-stride row in candidate order (group ballot).
 // The culling is conservative (a 1e-3 A margin); membership is decided by the
 // exact predicate alone.  The bead's native partners sit in registers.
+constexpr int kNlThreads = 256;
 template <bool UNI>
-__global__ void __launch_bounds__(256) k_nl(DevSys s) {
+__global__ void __launch_bounds__(kNlThreads) k_nl(DevSys s) {
   const int k = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) / kNlLanes);
   const int lane = threadIdx.x % kNlLanes;
   const unsigned wl = threadIdx.x & 31;
@@ -389,7 +390,8 @@ __global__ void __launch_bounds__(256) k_nl(DevSys s) {
 #pragma unroll
   for (int q = 0; q < kNatRegs; ++q) nat[q] = q < nrow.y ? s.nat_j[nrow.x + q] : -1;
   const long long stride = s.nl_stride;
-  int* row = s.nl_j + (long long)i * stride;
+  unsigned short* row = s.nl_j + (long long)i * stride;  // partners relative to the molecule start
+  const int mstart = s.mol[m].start;
   int cnt = 0;
   for (int z = z0; z <= z1; ++z) {
     const float dz = g.brute ? 0.0f : slab_dist(xi.z, g.lo[2] + z * g.cs, g.cs);
@@ -435,7 +437,7 @@ __global__ void __launch_bounds__(256) k_nl(DevSys s) {
         const unsigned msk = __ballot_sync(gmask, pass);
         if (pass) {
           const int pos = cnt + __popc(msk & below);
-          if (pos < stride) row[pos] = j;
+          if (pos < stride) row[pos] = (unsigned short)(j - mstart);
         }
         cnt += __popc(msk);
       }
@@ -480,22 +482,28 @@ __global__ void __launch_bounds__(256, 5) k_pl(DevSys s, int koff) {  // 48 regi
   const float r11 = s.rc2_pl_rep[1][1], r12 = s.rc2_pl_rep[1][2], r22 = s.rc2_pl_rep[2][2];
   const unsigned lt = (1u << lane) - 1u;
   const long long a = (long long)i * s.nl_stride;
-  const int4* row4 = reinterpret_cast<const int4*>(s.nl_j + a);
-  unsigned short* out = s.pl_j + a;  // partners relative to the molecule's first bead
+  // rows hold partners relative to the molecule's first bead, 4 per 8 bytes
+  const uint2* row4 = reinterpret_cast<const uint2*>(s.nl_j + a);
+  unsigned short* out = s.pl_j + a;
   const int mstart = s.mol[m].start;
+  const unsigned irel = (unsigned)(i - mstart);
+  const unsigned self2 = irel | (irel << 16);  // two entries that name bead i
   const int cnt = s.nl_cnt[i];
   const int2 row = s.nat_row[i];
   const int acnt = s.nl_att_cnt[i];
   int k = 0;
   // each round works on entries loaded the round before (rows are read ahead)
-  int4 jn = make_int4(i, i, i, i);
+  uint2 jn = make_uint2(self2, self2);
   if (4 * lane < cnt) jn = row4[lane];
   for (int e0 = 0; e0 < cnt; e0 += 4 * kPlLanes) {
     const int e = e0 + 4 * lane;
-    const int4 jv = jn;
-    jn = make_int4(i, i, i, i);
+    const uint2 jv = jn;
+    jn = make_uint2(self2, self2);
     if (e + 4 * kPlLanes < cnt) jn = row4[(e0 >> 2) + kPlLanes + lane];
-    const int jq[4] = {jv.x, e + 1 < cnt ? jv.y : i, e + 2 < cnt ? jv.z : i, e + 3 < cnt ? jv.w : i};
+    const int jq[4] = {mstart + (int)(jv.x & 0xffffu),
+                       e + 1 < cnt ? mstart + (int)(jv.x >> 16) : i,
+                       e + 2 < cnt ? mstart + (int)(jv.y & 0xffffu) : i,
+                       e + 3 < cnt ? mstart + (int)(jv.y >> 16) : i};
     unsigned pb = 0;
     int c = 0;
 #pragma unroll
@@ -586,7 +594,7 @@ static void launch_binning(const DevSys& s, const NLScratch& w, int koff, int at
 
 // Full neighbour-list rebuild from the coordinates at step mol_step + koff.
 void launch_nl_rebuild(const DevSys& s, const NLScratch& w, int koff, cudaStream_t st) {
-  const int T = 256;
+  const int T = kNlThreads;
   launch_binning(s, w, koff, 1, st);
   if (s.uniform_type)
     k_nl<true><<<cdiv((long long)s.nlive * kNlLanes, T), T, 0, st>>>(s);

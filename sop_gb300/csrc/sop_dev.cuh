@@ -12,11 +12,13 @@
 //                         rows of both of its beads ("full" lists), so each
 //                         bead sums its own force without atomics and the
 //                         summation order is fixed
-//   nl_j[nbead*stride] int repulsive neighbour list, fixed-stride rows: row i
-//                         starts at i*nl_stride (16-byte aligned), holds
-//                         nl_cnt[i] partners; a row that would outgrow the
-//                         stride raises the overflow flag and the host regrows
-//   pl_cnt, pl_j    int   repulsive pair list in the same row layout: row i
+//   nl_j[nbead*stride] u16 repulsive neighbour list, fixed-stride rows: row i
+//                         starts at i*nl_stride (64-byte aligned), holds
+//                         nl_cnt[i] partners, each as its index minus the
+//                         molecule's first bead (molecules hold at most
+//                         65,535 beads); a row that would outgrow the stride
+//                         raises the overflow flag and the host regrows
+//   pl_cnt, pl_j    u16   repulsive pair list in the same row layout: row i
 //                         is the first pl_cnt[i] entries at i*nl_stride (an
 //                         in-order compaction of the neighbour-list row)
 //   nl_att_cnt/nl_att_e   attractive neighbour list: native-entry indices in
@@ -91,11 +93,12 @@ struct DevSys {
 
   int* nl_att_cnt; int* nl_att_e;
   int* pl_att_cnt; float4* pl_att;
-  int* nl_cnt; int* nl_j; long long nl_stride;
+  int* nl_cnt;
+  unsigned short* nl_j;         // repulsive NL rows: partner - molecule start
+  long long nl_stride;
   int* nl_maxrow;               // largest row a rebuild needed (for regrowth)
   int* pl_cnt;
-  unsigned short* pl_j;         // repulsive PL rows: partner - molecule start (molecules
-                                // hold at most 65,535 beads), same row stride as nl_j
+  unsigned short* pl_j;         // repulsive PL rows, the same layout
 
   // neighbour-list build scratch
   unsigned* bbox;               // 6 per molecule, order-preserving float bits
