@@ -189,13 +189,14 @@ def launches_per_bench_step(p, s0: int, form: int = 1) -> int:
         nl = p.nnlup > 0 and st % p.nnlup == 0
         pl = nl or p.nplup <= 1 or st % p.nplup == 0
         n += (nl_kernels if nl else 0) + (1 if pl else 0)
+        n += 1 if nl and k > 0 else 0   # the clock advance ahead of a mid-block rebuild
         if form == 3:
             if pl or not in_run:
                 runs += 1
             in_run = True
         else:
             n += 2 if form == 2 else 1
-    return n + runs + 1   # step advance
+    return n + runs + 1   # the block's closing step advance
 
 
 def step_kernel_bytes(e, mols) -> tuple[float, dict]:

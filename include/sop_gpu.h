@@ -76,7 +76,7 @@ typedef struct sop_params {
   int rep6;           /* 0: eps (s^12/r^12 + s^6/r^6) as energy.cu:436-437; 1: eps (s/r)^6 */
   int device;         /* CUDA device ordinal (set device, param.cpp:387-390) */
   int graph_steps;    /* steps per captured CUDA graph (0: the engine's default) */
-  int lanes_per_bead; /* 0: autotuned table; else 1,2,4,8,16 or 32 */
+  int lanes_per_bead; /* 0: autotuned; else 2, 4, 8 or 16 (others: SOP_ERR_ARG) */
   unsigned long long seed; /* Philox key (replaces setup_rng's seed, GPUvars.cu:417-453) */
   int integrator;     /* 0: underdamped Langevin (sop.cu:421-462); 1: overdamped,
                          x += (h / zeta) f with f = F + noise (sop.cu:487-521,
@@ -99,6 +99,12 @@ typedef struct sop_params {
                          when the tuner times it faster than the best
                          whole-context step, 1: always (lanes and form must
                          be left to the tuner), < 0: never.  Same bits. */
+  int nl_rows;        /* initial length of the neighbour-list rows, entries
+                         (rounded up to a multiple of 32); 0: sized for the
+                         densest synthetic globules (1.3 x 6e-3 beads / A^3
+                         within the largest cut-off, at most the largest
+                         molecule).  A row that outgrows it regrows the rows,
+                         at commit, at an upload or mid-run. */
 } sop_params;
 
 /* Fills *p with the reference's defaults and the factor-mode list cut-offs. */

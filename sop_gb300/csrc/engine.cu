@@ -16,6 +16,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <memory>
 #include <numeric>
 #include <string>
 #include <thread>
@@ -354,6 +355,10 @@ constexpr int kMaxMolBeads = 65535;    // 16-bit molecule-relative pair-list par
 // fixed by the parameters; results are bit-identical for every G, form and
 // window, so only the speed differs.  A fixed window or the persistent form
 // (step_window > 0, step_split = 3) is timed as given.
+// Timed launches per tuning candidate (after one warm-up): step times repeat
+// to about 1%, and the candidates the tuner separates differ by more.
+constexpr int kTuneReps = 2;
+
 int autotune_lanes(SopCtx* ctx) {
   const int fixed_g = lanes_for(ctx), fixed_f = split_for(ctx), fixed_w = window_param(ctx);
   const int cand[4] = {2, 4, 8, 16};
@@ -381,8 +386,8 @@ int autotune_lanes(SopCtx* ctx) {
       const bool sp = f == 2;
       for (int wc : wins) {
         if (f == 3 && wc != 0) continue;
-        // three force-only evaluations (idempotent): three launches, or one
-        // persistent launch with barriers between them
+        // kTuneReps force-only evaluations (idempotent): as many launches,
+        // or one persistent launch with barriers between them
         auto run = [&](int reps) -> cudaError_t {
           if (f == 3)
             return launch_step_persist(ctx->s, g, 0, reps, false, barrier_words(ctx),
@@ -392,12 +397,12 @@ int autotune_lanes(SopCtx* ctx) {
         };
         CK(run(1));  // warm-up
         CK(cudaEventRecord(a, ctx->stream));
-        CK(run(3));
+        CK(run(kTuneReps));
         CK(cudaEventRecord(b, ctx->stream));
         CK(cudaEventSynchronize(b));
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, a, b));
-        gbest = std::min(gbest, ms / 3.0f);
+        gbest = std::min(gbest, ms / (float)kTuneReps);
         if (ms < best) { best = ms; bestg = g; bestf = f; bestw = wc; }
       }
     }
@@ -497,21 +502,30 @@ int rebuilds_before(const sop_params& P, long long n) {
   return r;
 }
 
-// Launch sequence of steps s0+1 .. s0+count (koff 0 .. count-1) and the
-// step-count advance.
+// Launch sequence of steps s0+1 .. s0+count and the step-count advance.
+// The clocks advance ahead of every neighbour-list rebuild by the steps run
+// since the last advance, and koff counts from there: a rebuild that
+// overflows the rows then stops every later kernel of the block with the
+// clocks at the rebuild, and the steps before it, already done, are not run
+// again when the host regrows the rows and replays from the clock.
 void enqueue_block(SopCtx* ctx, long long s0, int count) {
   int run0 = 0;  // first step of the current run without rebuilds
+  int base = 0;  // steps of the block the clocks already count
   for (int k = 0; k < count; ++k) {
     int r = rebuilds_before(ctx->P, s0 + 1 + k);
     if (r) {
-      launch_steps(ctx, run0, k - run0);
+      launch_steps(ctx, run0 - base, k - run0);
       run0 = k;
     }
-    if (r & 1) launch_nl_rebuild(ctx->s, ctx->w, k, ctx->stream);
-    if (r & 2) launch_pl_rebuild(ctx->s, k, ctx->stream);
+    if ((r & 1) && k > base) {
+      launch_advance(ctx->s, k - base, ctx->stream);
+      base = k;
+    }
+    if (r & 1) launch_nl_rebuild(ctx->s, ctx->w, k - base, ctx->stream);
+    if (r & 2) launch_pl_rebuild(ctx->s, k - base, ctx->stream);
   }
-  launch_steps(ctx, run0, count - run0);
-  launch_advance(ctx->s, count, ctx->stream);
+  launch_steps(ctx, run0 - base, count - run0);
+  launch_advance(ctx->s, count - base, ctx->stream);
 }
 
 int graph_for(SopCtx* ctx, long long s0, int count, cudaGraphExec_t* out) {
@@ -590,8 +604,9 @@ int sync_checked(SopCtx* ctx) {
     CK(cudaStreamSynchronize(ctx->stream));
     if (flags & FLAG_BARRIER_TIMEOUT) return barrier_failure(ctx);
     if (!(flags & FLAG_NL_OVERFLOW)) return SOP_OK;
-    // Every molecule froze at the start of the block that overflowed; the
-    // context's clock stopped there too.
+    // Every molecule froze at the neighbour-list rebuild that overflowed,
+    // and the context's clock with them (enqueue_block advances the clocks
+    // ahead of each such rebuild).
     long long done = 0;
     CK(cudaMemcpy(&done, ctx->s.sys_step, sizeof(long long), cudaMemcpyDeviceToHost));
     int rc = grow_nl(ctx);
@@ -765,14 +780,33 @@ int alloc_pools(SopCtx* ctx, const Caps& c) {
 // consecutive pool ranges (beads [o, o + n), bond / angle / native entries
 // from ob / oa / on, molecule slots from slot0), uploaded with one copy per
 // array.
+// A host array that is sized without being cleared: every entry of a staged
+// array is written by fill_rows (the ranges of the staged molecules tile it),
+// so clearing tens of MB first would only cost time.
+template <class T>
+struct RawArray {
+  std::unique_ptr<T[]> p;
+  size_t n = 0;
+  void reset(size_t k) {
+    p.reset(k ? new T[k] : nullptr);  // default-initialised: not cleared
+    n = k;
+  }
+  T* data() { return p.get(); }
+  const T* data() const { return p.get(); }
+  size_t size() const { return n; }
+  bool empty() const { return n == 0; }
+  T& operator[](size_t i) { return p[i]; }
+  const T& operator[](size_t i) const { return p[i]; }
+};
+
 struct Staged {
   long long o = 0, ob = 0, oa = 0, on = 0;
   int slot0 = 0;
-  std::vector<int2> brow, arow, nrow;
-  std::vector<int> bj, aj, nj, molof;
-  std::vector<float> br;
-  std::vector<float4> np, x0, p0, v0;
-  std::vector<float2> nr;
+  RawArray<int2> brow, arow, nrow;
+  RawArray<int> bj, aj, nj, molof;
+  RawArray<float> br;
+  RawArray<float4> np, x0, p0, v0;
+  RawArray<float2> nr;
   std::vector<long long> step0;
   std::vector<MolConst> mc;
   long long beads() const { return (long long)x0.size(); }
@@ -867,12 +901,12 @@ void fill_rows(const SopCtx* ctx, const HostMol& hm, int k, long long step0, Sta
 void size_staged(Staged& S, long long o, long long ob, long long oa, long long on, int slot0,
                  long long beads, long long b2, long long a2, long long n2, int nm) {
   S.o = o; S.ob = ob; S.oa = oa; S.on = on; S.slot0 = slot0;
-  S.brow.assign(beads, int2{}); S.arow.assign(beads, int2{}); S.nrow.assign(beads, int2{});
-  S.molof.assign(beads, 0);
-  S.x0.assign(beads, float4{}); S.p0.assign(beads, float4{}); S.v0.assign(beads, float4{});
-  S.bj.assign(b2, 0); S.br.assign(b2, 0.f);
-  S.aj.assign(a2, 0);
-  S.nj.assign(n2, 0); S.np.assign(n2, float4{}); S.nr.assign(n2, float2{});
+  S.brow.reset(beads); S.arow.reset(beads); S.nrow.reset(beads);
+  S.molof.reset(beads);
+  S.x0.reset(beads); S.p0.reset(beads); S.v0.reset(beads);
+  S.bj.reset(b2); S.br.reset(b2);
+  S.aj.reset(a2);
+  S.nj.reset(n2); S.np.reset(n2); S.nr.reset(n2);
   S.mc.assign(nm, MolConst{});
   S.step0.assign(nm, 0);
 }
@@ -985,11 +1019,11 @@ int time_step(SopCtx* ctx, bool tiles, int ntiles, bool any_split, float* ms) {
   };
   run();  // warm-up
   CK(cudaEventRecord(a, ctx->stream));
-  for (int r = 0; r < 3; ++r) run();
+  for (int r = 0; r < kTuneReps; ++r) run();
   CK(cudaEventRecord(b, ctx->stream));
   CK(cudaEventSynchronize(b));
   CK(cudaEventElapsedTime(ms, a, b));
-  *ms /= 3.0f;
+  *ms /= (float)kTuneReps;
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   CK(cudaGetLastError());
@@ -1087,6 +1121,19 @@ int setup_step0(SopCtx* ctx) {
   return SOP_OK;
 }
 
+// Neighbour-list row length for molecules of up to max_beads beads: the
+// parameter nl_rows where it is set, else 1.3 x
+// the neighbours of a bead in the densest part of a globule (6e-3 / A^3: the
+// cores of the synthetic structures reach about twice their mean density of
+// 2.5e-3), and no more than a molecule holds.
+long long dense_stride(const SopCtx* ctx, long long max_beads) {
+  if (ctx->P.nl_rows > 0) return std::max<long long>(64, ((long long)ctx->P.nl_rows + 31) / 32 * 32);
+  const double rc_nl = ctx->s.rc_nl_rep_max;
+  long long stride = (long long)(1.3 * 6.0e-3 * 4.18879 * rc_nl * rc_nl * rc_nl) + 32;
+  stride = std::min<long long>(stride, max_beads + 32);
+  return std::max<long long>(64, (stride + 31) / 32 * 32);
+}
+
 // Packs every staged molecule into exactly sized pools (plain and batched
 // contexts): molecule id = slot, all at step 0.
 int commit(SopCtx* ctx) {
@@ -1102,7 +1149,10 @@ int commit(SopCtx* ctx) {
   }
   c.mols = (long long)ctx->mols.size();
   if (c.beads <= 0) return ctx->fail(SOP_ERR_ARG, "no beads");
-  c.stride = 64;  // regrown from the first rebuild's longest row
+  // rows sized so that most contexts never regrow them (a regrowth costs a
+  // second list build at commit); a longer row regrows from the first
+  // rebuild's longest one
+  c.stride = dense_stride(ctx, c.max_mol_beads);
   int rc = alloc_pools(ctx, c);
   if (rc) return rc;
   ctx->s.uniform_type = 1;
@@ -1194,6 +1244,7 @@ void sop_params_default(sop_params* p) {
   p->step_split = 0;    // autotuned
   p->step_window = 0;   // autotuned
   p->step_buckets = 0;  // autotuned
+  p->nl_rows = 0;       // sized for dense globules
 }
 
 int sop_ctx_create(const sop_params* p, void** out) {
@@ -1201,6 +1252,8 @@ int sop_ctx_create(const sop_params* p, void** out) {
   *out = nullptr;
   if (p->boxl <= 0 || p->h <= 0 || p->R0 <= 0 || p->graph_steps < 0 || p->integrator < 0 ||
       p->step_split < 0 || p->step_split > 3 || p->step_window > kMaxStepWindow ||
+      !(p->lanes_per_bead == 0 || p->lanes_per_bead == 2 || p->lanes_per_bead == 4 ||
+        p->lanes_per_bead == 8 || p->lanes_per_bead == 16) || p->nl_rows < 0 ||
       p->integrator > 1 || (p->integrator == 1 && p->zeta <= 0)) {
     g_lib_error = "invalid parameters";
     return SOP_ERR_ARG;
@@ -1651,12 +1704,7 @@ int sop_serve_create(const sop_params* p, long long budget_bytes, long long max_
   int P = graph_steps(ctx);
   if (ctx->P.nnlup % P) ctx->P.graph_steps = std::gcd(P, ctx->P.nnlup);
   set_constants(ctx);
-  // list rows: 1.3 x the neighbours of a bead in the densest part of a
-  // globule (6e-3 / A^3: the cores of the synthetic structures reach about
-  // twice their mean density of 2.5e-3), so rows rarely have to regrow
-  const double rc_nl = ctx->s.rc_nl_rep_max;
-  long long stride = (long long)(1.3 * 6.0e-3 * 4.18879 * rc_nl * rc_nl * rc_nl) + 32;
-  stride = std::max<long long>(64, (stride + 31) / 32 * 32);
+  const long long stride = dense_stride(ctx, max_job_beads);
   // bytes per bead slot: state (8 float4), counters and cell data (10 ints),
   // rows (3 int2), topology (2 bond, 2 angle, 8 native entries) and list rows
   // (neighbour and pair list, 16-bit entries)

@@ -52,7 +52,8 @@ class Params(ctypes.Structure):
                 ("device", ctypes.c_int), ("graph_steps", ctypes.c_int),
                 ("lanes_per_bead", ctypes.c_int), ("seed", ctypes.c_ulonglong),
                 ("integrator", ctypes.c_int), ("step_split", ctypes.c_int),
-                ("step_window", ctypes.c_int), ("step_buckets", ctypes.c_int)]
+                ("step_window", ctypes.c_int), ("step_buckets", ctypes.c_int),
+                ("nl_rows", ctypes.c_int)]
 
 
 class MoleculeDesc(ctypes.Structure):

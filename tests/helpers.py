@@ -28,6 +28,22 @@ def force_error(f, fo):
     return float((np.linalg.norm(f - fo, axis=1) / np.maximum(mag, floor)).max())
 
 
+def force_error_report(f, fo):
+    """The floored metric of force_error beside what the floor hides: the
+    unfloored max relative error, how many beads sit below the floor, and the
+    largest absolute error as a fraction of the RMS bead force."""
+    f = np.asarray(f, np.float64)
+    fo = np.asarray(fo, np.float64)
+    mag = np.linalg.norm(fo, axis=1)
+    rms = np.sqrt((mag ** 2).mean())
+    floor = 1e-3 * rms
+    d = np.linalg.norm(f - fo, axis=1)
+    return {"floored": float((d / np.maximum(mag, floor)).max()),
+            "unfloored": float((d / np.maximum(mag, 1e-300)).max()),
+            "beads_below_floor": int((mag < floor).sum()), "beads": int(len(mag)),
+            "abs_max_over_rms": float(d.max() / rms)}
+
+
 def oracle_lists(mol, x, p, boxl=500.0):
     """Oracle NL and PL (att as native indices, rep as (i, j)) for engine params p."""
     nl_att = O.filter_att(mol, x, None, p.nl_att_fac, p.nl_att_abs, boxl)

@@ -42,6 +42,19 @@ def test_params_default_matches_reference():
     assert (p.nl_att_fac, p.nl_rep_fac, p.pl_att_fac, p.pl_rep_fac) == (3.2, 3.2, 2.5, 2.5)
 
 
+@pytest.mark.parametrize("field,value", [("lanes_per_bead", 3), ("lanes_per_bead", 32),
+                                         ("step_split", 4), ("h", 0.0), ("boxl", -1.0)])
+def test_context_refuses_invalid_parameters(field, value):
+    """Parameters are checked before any device is touched: an invalid one is
+    SOP_ERR_ARG with a message, and no context is made."""
+    p = engine.default_params()
+    setattr(p, field, value)
+    h = ctypes.c_void_p()
+    rc = engine.lib().sop_ctx_create(ctypes.byref(p), ctypes.byref(h))
+    assert rc == 1 and not h.value  # SOP_ERR_ARG
+    assert b"invalid parameters" in engine.lib().sop_last_error(None)
+
+
 @pytest.mark.parametrize("n,seed", [(128, 0), (4000, 1)])
 def test_generator_meets_spec(n, seed):
     m = system.generate(n, seed)

@@ -10,7 +10,7 @@
 import numpy as np
 import pytest
 
-from helpers import att_sel, force_error, oracle_lists
+from helpers import att_sel, force_error, force_error_report, oracle_lists
 from oracle import pyoracle as O
 from sop_gb300 import engine, system
 
@@ -44,7 +44,9 @@ def check_lists_and_forces(e, mol, x, p, boxl):
     e.set_noise(None)
     fo, _ = O.forces_f64(mol, x, att_sel(mol, pai, paj), pri, prj)
     err = force_error(f, fo)
-    assert err <= FORCE_TOL, err
+    rep = force_error_report(f, fo)
+    print(n, rep)
+    assert err <= FORCE_TOL, (err, rep)
     return len(ri), len(pri)
 
 

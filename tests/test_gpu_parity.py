@@ -8,7 +8,7 @@ bead force).  Single steps: identical injected noise.
 import numpy as np
 import pytest
 
-from helpers import att_sel, force_error, oracle_lists, pairset
+from helpers import att_sel, force_error, force_error_report, oracle_lists, pairset
 from oracle import pyoracle as O
 from sop_gb300 import engine, system
 
@@ -83,7 +83,9 @@ def test_forces_vs_fp64(n, seed, mode, sigma):
         pri, prj, _ = e.list_pairs(0, 3)
     fo, _ = O.forces_f64(mol, x, att_sel(mol, pai, paj), pri, prj)
     err = force_error(f, fo)
-    assert err <= FORCE_TOL, err
+    rep = force_error_report(f, fo)
+    print(n, mode, sigma, rep)
+    assert err <= FORCE_TOL, (err, rep)
 
 
 def test_forces_per_contact_epsilon():
@@ -301,7 +303,9 @@ def test_state_upload_touches_only_its_molecule():
     other: a finished molecule keeps the lists of its last step (its energy
     is evaluated on them) and a running one continues bit-identically to a
     run alone, also when the upload's neighbour list overflows the row
-    stride and the rows regrow."""
+    stride and the rows regrow.  The rows are sized at commit for the
+    densest synthetic globules, so the overflow comes from the folded
+    structure shrunk to half its size (eight times as dense)."""
     a, b, c = mol_of(128, 0), mol_of(4000, 1), mol_of(300, 5)
     p = engine.baseline_params(boxl=40000.0)
     e = engine.Engine(p)
@@ -313,8 +317,10 @@ def test_state_upload_touches_only_its_molecule():
     assert e.status(0)[1] == 20 and e.status(1) == (0, 30)
     before = [e.energy(0), *e.list_pairs(0, 1), *e.list_pairs(0, 3), *e.list_pairs(2, 3)]
     bytes0 = e.memory(0)[0]
-    e.upload_state(1, b.xyz)          # the folded structure: rows several times longer
+    dense = (b.xyz - b.xyz.mean(0)) * 0.5 + b.xyz.mean(0)
+    e.upload_state(1, dense.astype(np.float32))
     assert e.memory(0)[0] > bytes0    # the rows regrew
+    e.upload_state(1, b.xyz)          # the folded structure, in the regrown rows
     after = [e.energy(0), *e.list_pairs(0, 1), *e.list_pairs(0, 3), *e.list_pairs(2, 3)]
     for x, y in zip(after, before):
         np.testing.assert_array_equal(x, y)
@@ -331,6 +337,34 @@ def test_state_upload_touches_only_its_molecule():
         ref = alone.download()
     for k in ("unc_pos", "vel", "force"):
         np.testing.assert_array_equal(mixed[k], ref[k])
+
+
+def test_rows_regrow_mid_run():
+    """A neighbour-list row that outgrows the row stride at a rebuild inside a
+    running block of steps: every molecule freezes at the start of that block,
+    the rows regrow (keeping every molecule's lists) and the block runs again.
+    The trajectory is the one of a context whose rows had room from the
+    start, bit for bit.  The start is the folded 4,000-bead structure
+    expanded by 1.3 about its centre, moving inwards (v = -0.03 (x - c) per
+    unit time): its longest row grows from 289 entries at the start to
+    about 360 at step 50 and 540 at step 200, past rows of 320 entries and
+    then past the regrown ones."""
+    mol = system.generate(4000, 1)
+    c = mol.xyz.mean(0)
+    x0 = ((mol.xyz - c) * 1.3 + c).astype(np.float32)
+    v0 = (-0.03 * (x0 - c)).astype(np.float32)
+    with engine.plain(mol, x0, engine.baseline_params(nl_rows=300), T=0.6, traj=3, vel=v0) as e:
+        m0 = e.memory(0)[0]
+        e.step(300)
+        grown = e.memory(0)[0] > m0
+        assert e.status(0)[0] == 0
+        a = e.download()
+    with engine.plain(mol, x0, engine.baseline_params(), T=0.6, traj=3, vel=v0) as e:
+        e.step(300)
+        b = e.download()
+    assert grown
+    for k in ("unc_pos", "vel", "force"):
+        np.testing.assert_array_equal(a[k], b[k])
 
 
 @pytest.mark.parametrize("boxl", [40000.0, 500.0])
