@@ -41,9 +41,11 @@ __device__ __forceinline__ int warp_incl_scan(int v) {
 }
 
 // Block-wide exclusive scan of one value per thread; returns the exclusive
-// prefix and the block total in *total.
+// prefix and the block total in *total.  The total has its own slot: with
+// 1,024 threads all 32 warp slots hold prefixes.
 __device__ __forceinline__ int block_excl_scan(int v, int* total) {
   __shared__ int warp_sums[32];
+  __shared__ int block_total;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int incl = warp_incl_scan(v);
   if (lane == 31) warp_sums[w] = incl;
@@ -53,11 +55,11 @@ __device__ __forceinline__ int block_excl_scan(int v, int* total) {
     int s = lane < nw ? warp_sums[lane] : 0;
     int si = warp_incl_scan(s);
     if (lane < nw) warp_sums[lane] = si - s;
-    if (lane == 31) warp_sums[31] = si;  // total (nw <= 32)
+    if (lane == 31) block_total = si;
   }
   __syncthreads();
   int res = incl - v + warp_sums[w];
-  *total = warp_sums[31];
+  *total = block_total;
   __syncthreads();
   return res;
 }
@@ -108,13 +110,16 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int* __restri
 }
 
 // ---------------------------------------------------------------- grids
-__global__ void k_bbox_reset(DevSys s) {
-  int m = blockIdx.x * blockDim.x + threadIdx.x;
+// Each binning kernel's work per item is a device function, so that the
+// kernels below and the one-block binning of small contexts (k_bin_small)
+// share it.
+__device__ __forceinline__ void bbox_reset_at(const DevSys& s, int m) {
   if (m >= s.nmol) return;
   unsigned* b = s.bbox + 6 * m;
   b[0] = b[1] = b[2] = f2ord(INFINITY);
   b[3] = b[4] = b[5] = f2ord(-INFINITY);
 }
+__global__ void k_bbox_reset(DevSys s) { bbox_reset_at(s, blockIdx.x * blockDim.x + threadIdx.x); }
 
 // Molecules whose lists a rebuild at block offset koff refreshes: running,
 // healthy, and with the step this rebuild precedes (mol_step + koff + 1)
@@ -133,8 +138,8 @@ __device__ __forceinline__ const float4* xbuf(const DevSys& s, int m, int koff) 
   return s.x[(int)((s.mol_step[m] + koff) & 1)];
 }
 
-__global__ void k_bbox(DevSys s, int koff) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Called by all 32 lanes of a warp together (warp votes).
+__device__ __forceinline__ void bbox_at(const DevSys& s, int koff, int i) {
   int m = (i < s.nlive) ? s.mol_of[i] : -1;
   bool ok = mol_listed(s, m, koff);
   unsigned act = __ballot_sync(0xffffffffu, ok);
@@ -157,10 +162,10 @@ __global__ void k_bbox(DevSys s, int koff) {
     }
   }
 }
+__global__ void k_bbox(DevSys s, int koff) { bbox_at(s, koff, blockIdx.x * blockDim.x + threadIdx.x); }
 
 // One thread per molecule: cell grid of its neighbour-list build.
-__global__ void k_grid(DevSys s, int* __restrict__ ncell, int koff) {
-  int m = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void grid_at(const DevSys& s, int* ncell, int koff, int m) {
   if (m >= s.nmol) return;
   if (s.only_mol >= 0 && m != s.only_mol) {  // a rebuild of another molecule alone
     ncell[m] = 0;
@@ -174,11 +179,13 @@ __global__ void k_grid(DevSys s, int* __restrict__ ncell, int koff) {
     ncell[m] = 0;
     return;
   }
+  // the bounds come from atomics (performed in L2): read them from L2, so
+  // that a block that reset them itself cannot see its own stale L1 lines
   const unsigned* b = s.bbox + 6 * m;
   float lo[3], ext[3];
   for (int a = 0; a < 3; ++a) {
-    lo[a] = ord2f(b[a]);
-    ext[a] = ord2f(b[3 + a]) - lo[a];
+    lo[a] = ord2f(__ldcg(b + a));
+    ext[a] = ord2f(__ldcg(b + 3 + a)) - lo[a];
   }
   const float rc = s.rc_nl_rep_max;
   bool periodic = false;
@@ -229,12 +236,15 @@ __global__ void k_grid(DevSys s, int* __restrict__ ncell, int koff) {
   s.grid[m] = g;
   ncell[m] = g.ncell;
 }
+__global__ void k_grid(DevSys s, int* __restrict__ ncell, int koff) {
+  grid_at(s, ncell, koff, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // Single block: cell bases = exclusive scan of the per-molecule cell counts;
 // flags overflow of the cell capacity (cannot happen by construction: each
 // molecule holds at most max(64, 2n) cells, and the capacity is their sum).
-__global__ void __launch_bounds__(1024) k_grid_base(DevSys s, const int* __restrict__ ncell,
-                                                     int* __restrict__ cells_total) {
+// Called by every thread of one block.
+__device__ __forceinline__ void grid_base_block(const DevSys& s, const int* ncell, int* cells_total) {
   int carry = 0;
   for (int b0 = 0; b0 < s.nmol; b0 += blockDim.x) {
     int m = b0 + threadIdx.x;
@@ -249,6 +259,10 @@ __global__ void __launch_bounds__(1024) k_grid_base(DevSys s, const int* __restr
     *cells_total = carry > s.cell_cap ? (int)s.cell_cap : carry;
   }
 }
+__global__ void __launch_bounds__(1024) k_grid_base(DevSys s, const int* __restrict__ ncell,
+                                                     int* __restrict__ cells_total) {
+  grid_base_block(s, ncell, cells_total);
+}
 
 __device__ __forceinline__ int cell_coord(float v, float lo, float cs, int dim) {
   int c = (int)floorf((v - lo) / cs);
@@ -257,8 +271,7 @@ __device__ __forceinline__ int cell_coord(float v, float lo, float cs, int dim) 
 
 // Per bead: cell index and slot (counting sort), plus the attractive
 // neighbour-list filter of its native row (sop.cu:704-759 semantics).
-__global__ void k_assign(DevSys s, int koff, int att) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void assign_at(const DevSys& s, int koff, int att, int i) {
   if (i >= s.nlive) return;
   int m = s.mol_of[i];
   if (!mol_listed(s, m, koff)) {  // not binned; its lists stay as they are
@@ -298,21 +311,23 @@ __global__ void k_assign(DevSys s, int koff, int att) {
   }
   s.nl_att_cnt[i] = k;
 }
+__global__ void k_assign(DevSys s, int koff, int att) {
+  assign_at(s, koff, att, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
-__global__ void k_scatter(DevSys s) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void scatter_at(const DevSys& s, int i) {
   if (i >= s.nlive) return;
   int c = s.bead_cell[i];
   if (c < 0) return;
   s.sorted[s.cell_start[c] + s.bead_slot[i]] = i;
 }
+__global__ void k_scatter(DevSys s) { scatter_at(s, blockIdx.x * blockDim.x + threadIdx.x); }
 
 // Per cell: sort its beads by id (fixes every downstream order).  Cells hold
 // a handful of beads, so one thread's insertion sort is short.
-__global__ void k_cellsort(DevSys s, const int* __restrict__ cells_total) {
-  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void cellsort_at(const DevSys& s, const int* cells_total, long long c) {
   if (c >= *cells_total) return;
-  int cnt = s.cell_cnt[c];
+  int cnt = __ldcg(s.cell_cnt + c);  // counted by atomics: read from L2
   if (cnt == 0) return;
   int* b = s.sorted + s.cell_start[c];
   for (int a = 1; a < cnt; ++a) {
@@ -321,20 +336,75 @@ __global__ void k_cellsort(DevSys s, const int* __restrict__ cells_total) {
     b[k] = v;
   }
 }
+__global__ void k_cellsort(DevSys s, const int* __restrict__ cells_total) {
+  cellsort_at(s, cells_total, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // Coordinates staged in cell order, w = (id << 2) | type: a thread per
 // position, so the gathers are independent.
-__global__ void k_stage_xs(DevSys s, int koff) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void stage_xs_at(const DevSys& s, int koff, int k) {
   if (k >= s.cell_start[s.cell_cap]) return;  // beads that were binned
   const int i = s.sorted[k];
   float4 x = xbuf(s, s.mol_of[i], koff)[i];
   x.w = __int_as_float((i << 2) | type_of(x));
   s.xs[k] = x;
 }
+__global__ void k_stage_xs(DevSys s, int koff) { stage_xs_at(s, koff, blockIdx.x * blockDim.x + threadIdx.x); }
+
+// The whole binning in one block, for contexts small enough that the chain of
+// kernels above costs mostly launch latency: the same per-item work, phase
+// by phase, with block barriers between phases, so the same cells, order
+// and coordinates.  The scan of the cell counts runs over the block.
+constexpr int kBinThreads = 1024;
+constexpr long long kBinSmallCells = 1 << 16;
+//
+// Values that atomics produced in this kernel (the molecule bounds, the cell
+// counts) are read with __ldcg: atomics complete in L2, and the block's own
+// L1 may still hold the lines it cleared before them.
+__global__ void __launch_bounds__(kBinThreads) k_bin_small(DevSys s, int* ncell, int* cells_total,
+                                                           int koff, int att) {
+  const int t = threadIdx.x;
+  for (int m = t; m < s.nmol; m += kBinThreads) bbox_reset_at(s, m);
+  __syncthreads();
+  // every lane of a warp takes part in each round (warp votes)
+  for (int i0 = 0; i0 < s.nlive; i0 += kBinThreads) bbox_at(s, koff, i0 + t);
+  __syncthreads();
+  for (int m = t; m < s.nmol; m += kBinThreads) grid_at(s, ncell, koff, m);
+  __syncthreads();
+  grid_base_block(s, ncell, cells_total);
+  for (long long c = t; c < s.cell_cap; c += kBinThreads) s.cell_cnt[c] = 0;
+  __syncthreads();
+  for (int i = t; i < s.nlive; i += kBinThreads) assign_at(s, koff, att, i);
+  __syncthreads();
+  int carry = 0;  // exclusive scan of the cell counts into cell_start
+  for (long long c0 = 0; c0 < s.cell_cap; c0 += kBinThreads) {
+    const long long c = c0 + t;
+    const int v = c < s.cell_cap ? __ldcg(s.cell_cnt + c) : 0;
+    int total;
+    const int ex = block_excl_scan(v, &total);
+    if (c < s.cell_cap) s.cell_start[c] = carry + ex;
+    carry += total;
+  }
+  if (t == 0) s.cell_start[s.cell_cap] = carry;
+  __syncthreads();
+  for (int i = t; i < s.nlive; i += kBinThreads) scatter_at(s, i);
+  __syncthreads();
+  for (long long c = t; c < s.cell_cap; c += kBinThreads) cellsort_at(s, cells_total, c);
+  __syncthreads();
+  for (int k = t; k < s.nlive; k += kBinThreads) stage_xs_at(s, koff, k);
+}
+
+// The lanes of a group of L lanes (L divides 32) within its warp.
+template <int L>
+__device__ __forceinline__ unsigned group_mask(int wl) {
+  return L == 32 ? 0xffffffffu : (((1u << L) - 1u) << (wl & ~(L - 1)));
+}
+
+// Contexts of up to this many bead slots rebuild their lists with a warp
+// per bead: at 8 lanes per bead they fill less than a wave of the GPU.
+constexpr int kWideListBeads = 16384;
 
 constexpr int kNatRegs = 16;  // native partners held in registers (the rest are read)
-constexpr int kNlLanes = 8;
 
 // Distance from v to the slab [a, a + w] (0 inside).
 // cell_coord with a multiply by the inverse edge: for bounds that carry a
@@ -348,7 +418,8 @@ __device__ __forceinline__ float slab_dist(float v, float a, float w) {
   return fmaxf(fmaxf(a - v, v - (a + w)), 0.0f);
 }
 
-// kNlLanes lanes per bead, beads in cell order (xs), so neighbouring groups
+// L lanes per bead (8, or a warp for small contexts; the rows do not depend
+// on L), beads in cell order (xs), so neighbouring groups
 // share cells and candidates.  Each bead scans the cell rows (runs along x)
 // of its grid neighbourhood, culled against its own position: rows whose
 // y,z slab lies beyond the cut-off are skipped and each row's x range is
@@ -359,12 +430,12 @@ __device__ __forceinline__ float slab_dist(float v, float a, float w) {
 // The culling is conservative (a 1e-3 A margin); membership is decided by the
 // exact predicate alone.  The bead's native partners sit in registers.
 constexpr int kNlThreads = 256;
-template <bool UNI>
+template <bool UNI, int L>
 __global__ void __launch_bounds__(kNlThreads) k_nl(DevSys s) {
-  const int k = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) / kNlLanes);
-  const int lane = threadIdx.x % kNlLanes;
+  const int k = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) / L);
+  const int lane = threadIdx.x % L;
   const unsigned wl = threadIdx.x & 31;
-  const unsigned gmask = ((1u << kNlLanes) - 1u) << (wl & ~(kNlLanes - 1u));
+  const unsigned gmask = group_mask<L>((int)wl);
   const unsigned below = (1u << wl) - 1u;
   if (k >= s.cell_start[s.cell_cap]) return;   // beads that were binned
   if (*s.flags & FLAG_NL_OVERFLOW) return;
@@ -412,7 +483,7 @@ __global__ void __launch_bounds__(kNlThreads) k_nl(DevSys s) {
       const int rowc = g.base + (z * ny + y) * nx;
       const int ja = s.cell_start[rowc + xa];
       const int jb = s.cell_start[rowc + xb] + s.cell_cnt[rowc + xb];
-      for (int jc = ja; jc < jb; jc += kNlLanes) {
+      for (int jc = ja; jc < jb; jc += L) {
         const int jj = jc + lane;
         bool pass = false;
         int j = 0;
@@ -452,24 +523,25 @@ __global__ void __launch_bounds__(kNlThreads) k_nl(DevSys s) {
   }
 }
 
-// kPlLanes lanes per bead (four beads per warp): the pair list is the
-// in-order compaction of the bead's neighbour-list row by the pair-list
-// cut-off (sop.cu:835-920 semantics, host arithmetic of sop.cu:1737-1810).
-// Each lane takes 4 consecutive entries per round (one 16-byte load, four
-// independent gathers) and a scan across the group places the survivors;
-// the attractive pair list is the same over the bead's attractive
-// neighbour list.
-constexpr int kPlLanes = 8;   // lanes per bead in the pair-list rebuild
-template <bool UNI>
+// L lanes per bead (8: four beads per warp; 32: a warp per bead, for small
+// contexts, where fewer than a wave of beads leaves the latency of each
+// bead's rounds exposed): the pair list is the in-order compaction of the
+// bead's neighbour-list row by the pair-list cut-off (sop.cu:835-920
+// semantics, host arithmetic of sop.cu:1737-1810).  Each lane takes 4
+// consecutive entries per round (one 8-byte load, four independent gathers)
+// and a scan across the group places the survivors; the attractive pair
+// list is the same over the bead's attractive neighbour list.  The lists do
+// not depend on L.
+template <bool UNI, int L>
 __global__ void __launch_bounds__(256, 5) k_pl(DevSys s, int koff) {  // 48 registers: 5 blocks per SM
   pdl_wait();
   pdl_release();
   const int wl = threadIdx.x & 31;
-  const int lane = wl & (kPlLanes - 1);
-  const unsigned gmask = ((1u << kPlLanes) - 1u) << (wl & ~(kPlLanes - 1));
+  const int lane = wl & (L - 1);
+  const unsigned gmask = group_mask<L>(wl);
   // beads in chain order: the groups of a block gather from the same region
   // of a molecule, and the per-bead loads are coalesced
-  const int i = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) / kPlLanes);
+  const int i = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) / L);
   if (i >= s.nlive) return;
   if (*s.flags & FLAG_NL_OVERFLOW) return;
   const int m = s.mol_of[i];
@@ -480,7 +552,7 @@ __global__ void __launch_bounds__(256, 5) k_pl(DevSys s, int koff) {  // 48 regi
   const float boxl = s.boxl;
   const bool wrap = s.grid[m].wrap != 0;  // from the neighbour-list build, with a cut-off of margin
   const float r11 = s.rc2_pl_rep[1][1], r12 = s.rc2_pl_rep[1][2], r22 = s.rc2_pl_rep[2][2];
-  const unsigned lt = (1u << lane) - 1u;
+  const unsigned below = (1u << wl) - 1u;  // lanes of the warp before this one
   const long long a = (long long)i * s.nl_stride;
   // rows hold partners relative to the molecule's first bead, 4 per 8 bytes
   const uint2* row4 = reinterpret_cast<const uint2*>(s.nl_j + a);
@@ -495,11 +567,11 @@ __global__ void __launch_bounds__(256, 5) k_pl(DevSys s, int koff) {  // 48 regi
   // each round works on entries loaded the round before (rows are read ahead)
   uint2 jn = make_uint2(self2, self2);
   if (4 * lane < cnt) jn = row4[lane];
-  for (int e0 = 0; e0 < cnt; e0 += 4 * kPlLanes) {
+  for (int e0 = 0; e0 < cnt; e0 += 4 * L) {
     const int e = e0 + 4 * lane;
     const uint2 jv = jn;
     jn = make_uint2(self2, self2);
-    if (e + 4 * kPlLanes < cnt) jn = row4[(e0 >> 2) + kPlLanes + lane];
+    if (e + 4 * L < cnt) jn = row4[(e0 >> 2) + L + lane];
     const int jq[4] = {mstart + (int)(jv.x & 0xffffu),
                        e + 1 < cnt ? mstart + (int)(jv.x >> 16) : i,
                        e + 2 < cnt ? mstart + (int)(jv.y & 0xffffu) : i,
@@ -519,19 +591,19 @@ __global__ void __launch_bounds__(256, 5) k_pl(DevSys s, int koff) {  // 48 regi
     }
     int incl = c;
 #pragma unroll
-    for (int o = 1; o < kPlLanes; o <<= 1) {
-      const int t = __shfl_up_sync(gmask, incl, o, kPlLanes);
+    for (int o = 1; o < L; o <<= 1) {
+      const int t = __shfl_up_sync(gmask, incl, o, L);
       if (lane >= o) incl += t;
     }
     int pos = k + incl - c;
 #pragma unroll
     for (int q = 0; q < 4; ++q)
       if (pb & (1u << q)) out[pos++] = (unsigned short)(jq[q] - mstart);
-    k += __shfl_sync(gmask, incl, kPlLanes - 1, kPlLanes);
+    k += __shfl_sync(gmask, incl, L - 1, L);
   }
   if (lane == 0) s.pl_cnt[i] = k;
   int ka = 0;
-  for (int e0 = 0; e0 < acnt; e0 += kPlLanes) {
+  for (int e0 = 0; e0 < acnt; e0 += L) {
     const int e = e0 + lane;
     bool pass = false;
     int j = 0;
@@ -548,8 +620,8 @@ __global__ void __launch_bounds__(256, 5) k_pl(DevSys s, int koff) {  // 48 regi
       if (wrap) min_image3(dx, dy, dz, boxl);
       pass = d2_exact(dx, dy, dz) < rc2;
     }
-    const unsigned mask = (__ballot_sync(gmask, pass) >> (wl & ~(kPlLanes - 1))) & ((1u << kPlLanes) - 1u);
-    if (pass) s.pl_att[row.x + ka + __popc(mask & lt)] = make_float4(__int_as_float(j), q.x, q.y, q.z);
+    const unsigned mask = __ballot_sync(gmask, pass) & gmask;
+    if (pass) s.pl_att[row.x + ka + __popc(mask & below)] = make_float4(__int_as_float(j), q.x, q.y, q.z);
     ka += __popc(mask);
   }
   if (lane == 0) s.pl_att_cnt[i] = ka;
@@ -579,6 +651,10 @@ struct NLScratch {
 // the minimum image can matter), which the step and pair-list kernels read;
 // att = 1 also refreshes the attractive neighbour lists.
 static void launch_binning(const DevSys& s, const NLScratch& w, int koff, int att, cudaStream_t st) {
+  if (s.nlive <= kWideListBeads && s.cell_cap <= kBinSmallCells) {
+    k_bin_small<<<1, kBinThreads, 0, st>>>(s, w.ncell, w.cells_total, koff, att);
+    return;
+  }
   const int T = 256;
   k_bbox_reset<<<cdiv(s.nmol, T), T, 0, st>>>(s);
   k_bbox<<<cdiv(s.nlive, T), T, 0, st>>>(s, koff);
@@ -596,10 +672,15 @@ static void launch_binning(const DevSys& s, const NLScratch& w, int koff, int at
 void launch_nl_rebuild(const DevSys& s, const NLScratch& w, int koff, cudaStream_t st) {
   const int T = kNlThreads;
   launch_binning(s, w, koff, 1, st);
-  if (s.uniform_type)
-    k_nl<true><<<cdiv((long long)s.nlive * kNlLanes, T), T, 0, st>>>(s);
-  else
-    k_nl<false><<<cdiv((long long)s.nlive * kNlLanes, T), T, 0, st>>>(s);
+  const bool wide = s.nlive <= kWideListBeads;
+  const unsigned grid = cdiv((long long)s.nlive * (wide ? 32 : 8), T);
+  if (s.uniform_type) {
+    if (wide) k_nl<true, 32><<<grid, T, 0, st>>>(s);
+    else k_nl<true, 8><<<grid, T, 0, st>>>(s);
+  } else {
+    if (wide) k_nl<false, 32><<<grid, T, 0, st>>>(s);
+    else k_nl<false, 8><<<grid, T, 0, st>>>(s);
+  }
 }
 
 // The binning alone, every list untouched: molecules that arrive with their
@@ -612,10 +693,12 @@ void launch_rebin(const DevSys& s, const NLScratch& w, cudaStream_t st) {
 
 void launch_pl_rebuild(const DevSys& s, int koff, cudaStream_t st) {
   const int T = 256;
+  const bool wide = s.nlive <= kWideListBeads;
+  const unsigned grid = cdiv((long long)s.nlive * (wide ? 32 : 8), T);
   if (s.uniform_type)
-    launch_pdl(k_pl<true>, cdiv((long long)s.nlive * kPlLanes, T), T, st, s, koff);
+    launch_pdl(wide ? k_pl<true, 32> : k_pl<true, 8>, grid, T, st, s, koff);
   else
-    launch_pdl(k_pl<false>, cdiv((long long)s.nlive * kPlLanes, T), T, st, s, koff);
+    launch_pdl(wide ? k_pl<false, 32> : k_pl<false, 8>, grid, T, st, s, koff);
 }
 
 }  // namespace sop

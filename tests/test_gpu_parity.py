@@ -382,6 +382,28 @@ def test_extended_chain_lists(boxl):
     assert pairset(pri, prj) == pairset(opi, opj)
 
 
+def test_lists_of_more_than_a_thousand_molecules():
+    """The per-molecule cell bases come from a block-wide scan with 1,024
+    threads, one molecule per thread: 1,100 copies of a 1,000-bead molecule
+    in one context put molecules 992-1,023 in the block's last warp (whose
+    prefix a scan that kept its total in that warp's slot got wrong).  Every
+    copy's lists equal the oracle's."""
+    mol = mol_of(1000, 5)
+    p = engine.baseline_params()
+    ncopy = 1100
+    with engine.Engine(p) as e:
+        for k in range(ncopy):
+            e.add(mol, mol.xyz, T=0.6, traj=k)
+        e.commit()
+        nl_att, (nri, nrj), pl_att, (opi, opj) = oracle_lists(mol, mol.xyz, p)
+        want_nl, want_pl = pairset(nri, nrj), pairset(opi, opj)
+        for k in (0, 500, 991, 992, 1000, 1023, 1024, 1030, 1060, 1099):
+            ri, rj, _ = e.list_pairs(k, 1)
+            pri, prj, _ = e.list_pairs(k, 3)
+            assert pairset(ri, rj) == want_nl, k
+            assert pairset(pri, prj) == want_pl, k
+
+
 def test_batched_equals_alone():
     """Molecules packed into one context give bit-identical results to the
     same molecules run alone."""
