@@ -177,7 +177,7 @@ def whole_job_rate(beads_per_rank: int, md_steps: int, world: int, t_max: float)
 
 def launches_per_bench_step(p, s0: int, form: int = 1) -> int:
     """Kernels of the engine in one replay starting after step s0 (form 1:
-    one step kernel per step; 2: force + finish kernels; 3: one persistent
+    one step kernel per step; 2: force + finish kernels; 3 and 4: one
     launch per run of steps between list rebuilds)."""
     nl_kernels = 12    # bbox reset, bbox, grid, grid base, assign, 3 scan, scatter, cellsort,
                        # stage_xs, nl
@@ -190,7 +190,7 @@ def launches_per_bench_step(p, s0: int, form: int = 1) -> int:
         pl = nl or p.nplup <= 1 or st % p.nplup == 0
         n += (nl_kernels if nl else 0) + (1 if pl else 0)
         n += 1 if nl and k > 0 else 0   # the clock advance ahead of a mid-block rebuild
-        if form == 3:
+        if form in (3, 4):
             if pl or not in_run:
                 runs += 1
             in_run = True

@@ -84,8 +84,11 @@ typedef struct sop_params {
   int step_split;     /* form of the step: 1 one kernel, 2 a force kernel and a
                          finish kernel, 3 every step between two list rebuilds
                          in one cooperative launch (a device-wide barrier
-                         between steps), 0 chosen by timing at commit (served
-                         contexts: 2).  Every form gives the same bits. */
+                         between steps), 4 the same in one block of 1,024
+                         threads (block barriers; tried by the tuner for
+                         contexts of up to 2,048 bead slots), 0 chosen by
+                         timing at commit (served contexts: 2).  Every form
+                         gives the same bits. */
   int step_window;    /* shared-memory window of the step, in beads: each step
                          block stages the coordinates of its beads' molecules
                          (up to this many beads) and gathers partners from
@@ -272,7 +275,7 @@ int sop_memory(void* ctx, int mol, long long* ctx_bytes, long long* mol_bytes);
 int sop_tuning(void* ctx, int* lanes, float* ms);
 /* The step's shape in use: lanes per bead, and its form (1 one kernel, 2 a
  * force kernel and a finish kernel, 3 persistent: the steps between two list
- * rebuilds in one launch). */
+ * rebuilds in one cooperative launch, 4 the same in one block). */
 int sop_step_form(void* ctx, int* lanes, int* form);
 
 /* The per-size-bucket tiling of the step (sop_params.step_buckets): *tiled

@@ -41,6 +41,8 @@ long long scan_block_sums_needed(long long n);
 void launch_step(const DevSys& s, int G, bool split, int koff, bool step, int wcap,
                  cudaStream_t st);
 cudaError_t allow_step_window(int wcap);
+cudaError_t launch_step_block(const DevSys& s, int G, int koff0, int count, bool step,
+                              cudaStream_t st);
 cudaError_t launch_step_persist(const DevSys& s, int G, int koff0, int count, bool step,
                                 unsigned* bar, unsigned long long limit_ns, cudaStream_t st);
 cudaError_t launch_barrier_check(const DevSys& s, int G, unsigned* bar, int missing, int rounds,
@@ -197,6 +199,7 @@ struct SopCtx {
   bool split = false;         // step as force kernel + finish kernel
   int wcap = 0;               // > 0: step blocks stage their molecules (up to wcap beads)
   bool persist = false;       // steps between list rebuilds in one cooperative launch
+  bool one_block = false;     // steps between list rebuilds in one block
   // tiled form: per-molecule tiles, lanes and form chosen per size bucket
   bool tiled = false;
   int4* d_tiles = nullptr;    // {first bead, end bead, lanes, two-kernel form}
@@ -310,6 +313,8 @@ int grow_nl_keep(SopCtx* ctx, long long stride);
 
 namespace {
 
+int graph_steps(const SopCtx* ctx);
+
 // The rows of the molecule whose beads are o .. o + n - 1 in the repulsive
 // neighbour list (r = 0) or pair list (r = 1), every entry as an index
 // relative to bead o (as stored), full row stride.
@@ -331,11 +336,16 @@ int lanes_for(const SopCtx* ctx) {
 }
 
 // The step's form: 1 one kernel, 2 force kernel + finish kernel, 3 every
-// step between two list rebuilds in one cooperative launch, 0 autotuned.
+// step between two list rebuilds in one cooperative launch, 4 the same in
+// one block, 0 autotuned.
 int split_for(const SopCtx* ctx) {
   const int f = ctx->P.step_split;
-  return (f >= 1 && f <= 3) ? f : 0;
+  return (f >= 1 && f <= 4) ? f : 0;
 }
+
+// Contexts of up to this many bead slots let the tuner try the one-block
+// form (one SM does every bead: larger ones are faster spread over the GPU).
+constexpr int kOneBlockMaxBeads = 2048;
 
 // Wait limit of the persistent form's device-wide barrier: a step of the
 // largest context takes well under a millisecond.
@@ -373,6 +383,8 @@ int autotune_lanes(SopCtx* ctx) {
   cudaEvent_t a, b;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
+  // steps between two list rebuilds (the pair list's cadence, at most a graph)
+  const int run_len = std::max(1, std::min(graph_steps(ctx), ctx->P.nplup > 1 ? ctx->P.nplup : 1));
   float best = 1e30f;
   int bestg = fixed_g ? fixed_g : 8;
   int bestf = fixed_f ? fixed_f : 1;
@@ -380,29 +392,36 @@ int autotune_lanes(SopCtx* ctx) {
   for (int g : cand) {
     if (fixed_g && g != fixed_g) continue;
     float gbest = 1e30f;
-    for (int f = 1; f <= 3; ++f) {
-      if (fixed_f ? f != fixed_f : f == 3) continue;
-      if (f == 3 && ctx->served) continue;
+    for (int f = 1; f <= 4; ++f) {
+      if (fixed_f ? f != fixed_f : (f == 3 || (f == 4 && ctx->s.nlive > kOneBlockMaxBeads)))
+        continue;
+      if (f >= 3 && ctx->served) continue;
       const bool sp = f == 2;
       for (int wc : wins) {
-        if (f == 3 && wc != 0) continue;
+        if (f >= 3 && wc != 0) continue;
         // kTuneReps force-only evaluations (idempotent): as many launches,
-        // or one persistent launch with barriers between them
+        // or one persistent launch (with barriers between them)
         auto run = [&](int reps) -> cudaError_t {
           if (f == 3)
             return launch_step_persist(ctx->s, g, 0, reps, false, barrier_words(ctx),
                                        kBarrierLimitNs, ctx->stream);
+          if (f == 4) return launch_step_block(ctx->s, g, 0, reps, false, ctx->stream);
           for (int r = 0; r < reps; ++r) launch_step(ctx->s, g, sp, 0, false, wc, ctx->stream);
           return cudaGetLastError();
         };
+        // a form that runs every step between two rebuilds in one launch is
+        // timed over such a run (its launch is paid once per run); the
+        // others pay their launches per step, so two steps show their cost
+        const int reps = f == 4 ? run_len : kTuneReps;
         CK(run(1));  // warm-up
         CK(cudaEventRecord(a, ctx->stream));
-        CK(run(kTuneReps));
+        CK(run(reps));
         CK(cudaEventRecord(b, ctx->stream));
         CK(cudaEventSynchronize(b));
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, a, b));
-        gbest = std::min(gbest, ms / (float)kTuneReps);
+        ms /= (float)reps;  // per step
+        gbest = std::min(gbest, ms);
         if (ms < best) { best = ms; bestg = g; bestf = f; bestw = wc; }
       }
     }
@@ -417,6 +436,7 @@ int autotune_lanes(SopCtx* ctx) {
   ctx->G = bestg;
   ctx->split = bestf == 2;
   ctx->persist = bestf == 3;
+  ctx->one_block = bestf == 4;
   ctx->wcap = bestw;
   return SOP_OK;
 }
@@ -488,6 +508,10 @@ void launch_steps(SopCtx* ctx, int koff0, int count) {
   if (ctx->persist) {
     launch_step_persist(ctx->s, ctx->G, koff0, count, true, barrier_words(ctx), kBarrierLimitNs,
                         ctx->stream);
+    return;
+  }
+  if (ctx->one_block) {
+    launch_step_block(ctx->s, ctx->G, koff0, count, true, ctx->stream);
     return;
   }
   for (int k = koff0; k < koff0 + count; ++k)
@@ -1039,7 +1063,7 @@ int time_step(SopCtx* ctx, bool tiles, int ntiles, bool any_split, float* ms) {
 int autotune_buckets(SopCtx* ctx) {
   const int want = ctx->P.step_buckets;
   ctx->tiled = false;
-  if (want < 0 || ctx->served || ctx->persist || ctx->wcap > 0) return SOP_OK;
+  if (want < 0 || ctx->served || ctx->persist || ctx->one_block || ctx->wcap > 0) return SOP_OK;
   int present = 0;
   for (int b = 0; b < kBuckets; ++b) ctx->bucket_beads[b] = 0;
   long long cap = 0;
@@ -1095,6 +1119,7 @@ int setup_step0(SopCtx* ctx) {
   ctx->G = fixed_g ? fixed_g : 8;
   ctx->split = fixed_f == 2;
   ctx->persist = fixed_f == 3 && !ctx->served;
+  ctx->one_block = fixed_f == 4 && !ctx->served;
   ctx->wcap = 0;
   if (fixed_w > 0 && !ctx->served) {
     CK(allow_step_window(kMaxStepWindow));
@@ -1251,7 +1276,7 @@ int sop_ctx_create(const sop_params* p, void** out) {
   if (!p || !out) return SOP_ERR_ARG;
   *out = nullptr;
   if (p->boxl <= 0 || p->h <= 0 || p->R0 <= 0 || p->graph_steps < 0 || p->integrator < 0 ||
-      p->step_split < 0 || p->step_split > 3 || p->step_window > kMaxStepWindow ||
+      p->step_split < 0 || p->step_split > 4 || p->step_window > kMaxStepWindow ||
       !(p->lanes_per_bead == 0 || p->lanes_per_bead == 2 || p->lanes_per_bead == 4 ||
         p->lanes_per_bead == 8 || p->lanes_per_bead == 16) || p->nl_rows < 0 ||
       p->integrator > 1 || (p->integrator == 1 && p->zeta <= 0)) {
@@ -1736,6 +1761,7 @@ int sop_serve_create(const sop_params* p, long long budget_bytes, long long max_
   ctx->G = fixed_g ? fixed_g : 4;
   ctx->split = fixed_f != 1;
   ctx->persist = false;
+  ctx->one_block = false;
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->committed = true;
   ctx->host_step = 0;
@@ -2356,7 +2382,7 @@ int sop_step_form(void* p, int* lanes, int* form) {
   if (!p) return SOP_ERR_ARG;
   SopCtx* ctx = C(p);
   if (lanes) *lanes = ctx->G;
-  if (form) *form = ctx->persist ? 3 : ctx->split ? 2 : 1;
+  if (form) *form = ctx->one_block ? 4 : ctx->persist ? 3 : ctx->split ? 2 : 1;
   return SOP_OK;
 }
 

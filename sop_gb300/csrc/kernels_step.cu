@@ -588,6 +588,47 @@ __global__ void __launch_bounds__(kStepThreads, StepBlocks<G>::value)
   }
 }
 
+// One block of 1,024 threads runs every step between two list rebuilds:
+// for contexts of a few hundred beads, where each step is a short chain of
+// dependent loads and a kernel boundary (even overlapped by programmatic
+// dependent launch) costs as much as the step.  Steps are separated by
+// block barriers; the per-bead code is k_step's, so the bits are the same.
+constexpr int kBlockFormThreads = 1024;
+template <int G, bool STEP, bool UNI>
+__global__ void __launch_bounds__(kBlockFormThreads, 1) k_step_block(DevSys s, int koff0, int count) {
+  constexpr int BPB = kBlockFormThreads / G;
+  __shared__ float4 fsum[BPB];
+  __shared__ int bead[BPB];
+  pdl_wait();
+  pdl_release();
+  const int slot = threadIdx.x / G;
+  const int lane = threadIdx.x % G;
+  const int nchunks = (s.nlive + BPB - 1) / BPB;
+  for (int k = 0; k < count; ++k) {
+    // force-only evaluations (STEP = false, repeated for timing) recompute
+    // the same step, which keeps them idempotent
+    const int koff = STEP ? koff0 + k : koff0;
+    for (int c = 0; c < nchunks; ++c) {
+      const BeadSlot q = bead_slot<STEP>(s, c * BPB + slot, koff);
+      float fx = 0.f, fy = 0.f, fz = 0.f;
+      bool fene_bad = false;
+      if (q.i >= 0)
+        bead_force<G, UNI>(s, GlobalX{s.x[(int)(q.n & 1)]}, q.i, q.m1, lane, q.br, q.ar, q.abase,
+                           q.acnt, q.rcnt, fx, fy, fz, fene_bad);
+      if (lane == 0) {
+        fsum[slot] = marked_sum(fx, fy, fz, fene_bad, q.n);
+        bead[slot] = q.i;
+      }
+      __syncthreads();
+      if (threadIdx.x < BPB) {
+        const int b = bead[threadIdx.x];
+        if (b >= 0) finish_bead<STEP>(s, b, s.mol_of[b], fsum[threadIdx.x], koff);
+      }
+      __syncthreads();
+    }
+  }
+}
+
 // The barrier alone, for the check that its wait ends: `rounds` barriers
 // with `expected` arrivals (gridDim.x completes them; more makes every block
 // wait out the limit).
@@ -902,6 +943,27 @@ cudaError_t launch_step_persist(const DevSys& s, int G, int koff0, int count, bo
     case 4: return launch_persist_g<4>(s, koff0, count, step, bar, limit_ns, st);
     case 16: return launch_persist_g<16>(s, koff0, count, step, bar, limit_ns, st);
     default: return launch_persist_g<8>(s, koff0, count, step, bar, limit_ns, st);
+  }
+}
+
+template <int G>
+static cudaError_t launch_block_g(const DevSys& s, int koff0, int count, bool step, cudaStream_t st) {
+  if (s.uniform_type) {
+    if (step) return launch_pdl(k_step_block<G, true, true>, 1, kBlockFormThreads, st, s, koff0, count);
+    return launch_pdl(k_step_block<G, false, true>, 1, kBlockFormThreads, st, s, koff0, count);
+  }
+  if (step) return launch_pdl(k_step_block<G, true, false>, 1, kBlockFormThreads, st, s, koff0, count);
+  return launch_pdl(k_step_block<G, false, false>, 1, kBlockFormThreads, st, s, koff0, count);
+}
+
+// Steps koff0 .. koff0 + count - 1 (no list rebuild among them) in one block.
+cudaError_t launch_step_block(const DevSys& s, int G, int koff0, int count, bool step,
+                              cudaStream_t st) {
+  switch (G) {
+    case 2: return launch_block_g<2>(s, koff0, count, step, st);
+    case 4: return launch_block_g<4>(s, koff0, count, step, st);
+    case 16: return launch_block_g<16>(s, koff0, count, step, st);
+    default: return launch_block_g<8>(s, koff0, count, step, st);
   }
 }
 

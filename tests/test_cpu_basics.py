@@ -43,7 +43,7 @@ def test_params_default_matches_reference():
 
 
 @pytest.mark.parametrize("field,value", [("lanes_per_bead", 3), ("lanes_per_bead", 32),
-                                         ("step_split", 4), ("h", 0.0), ("boxl", -1.0)])
+                                         ("step_split", 5), ("h", 0.0), ("boxl", -1.0)])
 def test_context_refuses_invalid_parameters(field, value):
     """Parameters are checked before any device is touched: an invalid one is
     SOP_ERR_ARG with a message, and no context is made."""

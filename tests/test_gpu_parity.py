@@ -429,13 +429,13 @@ def test_batched_equals_alone():
 def test_lanes_per_bead_bit_identical():
     """The force summation order does not depend on the lanes per bead, and
     every form of the step (one kernel; force + finish kernels; the steps
-    between two rebuilds in one persistent launch) completes a bead with the
-    same code, so trajectories are bit-identical for every G and form (both
-    can be tuned freely)."""
+    between two rebuilds in one persistent launch, over the grid or in one
+    block) completes a bead with the same code, so trajectories are
+    bit-identical for every G and form (both can be tuned freely)."""
     mol = mol_of(4000, 1)
     outs = []
     for g in (2, 4, 8, 16):
-        for form in (1, 2, 3):
+        for form in (1, 2, 3, 4):
             p = engine.baseline_params(lanes_per_bead=g, step_split=form)
             with engine.plain(mol, mol.xyz, p, T=0.6, traj=2) as e:
                 t = e.tuning()
@@ -445,6 +445,25 @@ def test_lanes_per_bead_bit_identical():
     for o in outs[1:]:
         for k in ("unc_pos", "vel", "force"):
             np.testing.assert_array_equal(o[k], outs[0][k])
+
+
+def test_one_block_form_small_context():
+    """The one-block form on a context it is meant for (128 beads, every lane
+    count): bit-identical to the one-kernel form over 120 steps (list
+    rebuilds included), and the tuner may pick it."""
+    mol = mol_of(128, 0)
+    outs = []
+    for g, form in ((16, 1), (2, 4), (4, 4), (8, 4), (16, 4)):
+        p = engine.baseline_params(lanes_per_bead=g, step_split=form)
+        with engine.plain(mol, mol.xyz, p, T=0.6, traj=4) as e:
+            assert e.tuning()["form"] == form
+            e.step(120)
+            outs.append(e.download())
+    for o in outs[1:]:
+        for k in ("unc_pos", "vel", "force"):
+            np.testing.assert_array_equal(o[k], outs[0][k])
+    with engine.plain(mol, mol.xyz, engine.baseline_params(), T=0.6, traj=4) as e:
+        assert e.tuning()["form"] in (1, 2, 4)
 
 
 def test_step_window_bit_identical():
@@ -529,7 +548,7 @@ def test_autotune_picks_a_candidate():
     mol = mol_of(4000, 1)
     with engine.plain(mol, mol.xyz, engine.baseline_params()) as e:
         t = e.tuning()
-    assert t["lanes_per_bead"] in (2, 4, 8, 16) and t["form"] in (1, 2, 3)
+    assert t["lanes_per_bead"] in (2, 4, 8, 16) and t["form"] in (1, 2, 3, 4)
     assert all(v > 0 for v in t["ms"].values())
 
 

@@ -104,3 +104,23 @@ def test_submit_rejects_oversized_and_stepless_jobs():
             srv.submit(mol_of(700, 32), nsteps=10)
         with pytest.raises(engine.SopError):
             srv.submit(mol_of(220, 31), nsteps=-1)
+
+
+def test_more_than_a_thousand_jobs_at_once():
+    """1,100 jobs resident at once: the molecule slots run past the last warp
+    of the 1,024-thread scan of per-molecule cell bases (slots 992-1,023),
+    and jobs there must still equal their runs alone."""
+    p = params()
+    m = mol_of(150, 41)
+    njob = 1100
+    with engine.Server(p, budget_bytes=2 << 30, max_job_beads=1500) as srv:
+        ids = [srv.submit(m, m.xyz, nsteps=60, T=0.6, traj=1000 + k) for k in range(njob)]
+        srv.advance(1)
+        assert srv.stats()["active"] == njob
+        srv.run_until_idle()
+        for k in (0, 991, 992, 1000, 1023, 1024, 1099):
+            r = srv.result(ids[k])
+            unc, vel, _, _ = alone(150, 41, 60, 0.6, False, 1000 + k, p)
+            assert r["status"] == engine.MOL_DONE, k
+            np.testing.assert_array_equal(r["unc_pos"], unc)
+            np.testing.assert_array_equal(r["vel"], vel)
