@@ -373,29 +373,48 @@ __global__ void __launch_bounds__(kStepThreads, StepBlocks<G>::value) k_step(Dev
   finish_bead<STEP>(s, b, s.mol_of[b], fsum[threadIdx.x], koff);
 }
 
-// Completes bead b (of molecule m) from its conservative force sum fs, whose
-// w holds the marker bits k_step set: noise, status, velocity and the
-// look-ahead position update (sop.cu:421-462, energy.cu:588-604).  The step
-// is the molecule's mol_step + STEP + koff, as in k_step.  Every load is
-// issued before any store (they are independent), and every rounding is
-// written out.
-template <bool STEP>
-__device__ __forceinline__ void finish_bead(const DevSys& s, int b, int m, float4 fs, int koff) {
-  const int w = __float_as_int(fs.w);
-  const int cur = (w & kOddStep) ? 1 : 0;
-  const MolConst mc = s.mol[m];
-  const long long nb = s.mol_step[m] + (STEP ? 1 : 0) + koff;
-  float4 vi = s.v[b];
-  float4 inc = s.incr[b];
-  const float4 xo = s.x[cur][b];
-  const float4 pi = s.p[cur][b];
+// What completing bead b (of molecule m) at step mol_step + STEP + koff needs
+// besides its force sum: its state (coordinates from buffer cur, the step's
+// parity) and its noise.  None of it is written by the force kernel of the
+// same step.
+struct BeadState {
+  MolConst mc;
+  long long nb;
+  float4 vi, inc, xo, pi;
   float3 z;
+};
+
+template <bool STEP>
+__device__ __forceinline__ void load_bead_state(const DevSys& s, int b, int m, int koff, int cur,
+                                                BeadState& t) {
+  t.mc = s.mol[m];
+  t.nb = s.mol_step[m] + (STEP ? 1 : 0) + koff;
+  t.vi = s.v[b];
+  t.inc = s.incr[b];
+  t.xo = s.x[cur][b];
+  t.pi = s.p[cur][b];
   if (s.use_noise) {
     const float4 q = s.noise[b];
-    z = make_float3(q.x, q.y, q.z);
+    t.z = make_float3(q.x, q.y, q.z);
   } else {
-    z = noise3((unsigned)(b - mc.start), nb, mc.traj, s.seed_lo, s.seed_hi);
+    t.z = noise3((unsigned)(b - t.mc.start), t.nb, t.mc.traj, s.seed_lo, s.seed_hi);
   }
+}
+
+// Completes bead b from its conservative force sum fs, whose w holds the
+// marker bits k_step set: noise, status, velocity and the look-ahead
+// position update (sop.cu:421-462, energy.cu:588-604).  Every rounding is
+// written out.
+template <bool STEP>
+__device__ __forceinline__ void complete_bead(const DevSys& s, int b, int m, float4 fs, int cur,
+                                              const BeadState& t) {
+  const int w = __float_as_int(fs.w);
+  const MolConst& mc = t.mc;
+  float4 vi = t.vi;
+  float4 inc = t.inc;
+  const float4 xo = t.xo;
+  const float4 pi = t.pi;
+  const float3 z = t.z;
   const float fxx = __fmaf_rn(mc.sigma_f, z.x, fs.x);
   const float fyy = __fmaf_rn(mc.sigma_f, z.y, fs.y);
   const float fzz = __fmaf_rn(mc.sigma_f, z.z, fs.z);
@@ -405,7 +424,7 @@ __device__ __forceinline__ void finish_bead(const DevSys& s, int b, int m, float
   if (st) atomicOr(s.mol_status + m, st);
   s.f[b] = make_float4(fxx, fyy, fzz, 0.f);
   // step 0 is the initial force evaluation (sop.cu:180-186): velocities stay
-  if (STEP && nb > 0 && !mc.t_zero) {
+  if (STEP && t.nb > 0 && !mc.t_zero) {
     vi = make_float4(__fmaf_rn(mc.a3, inc.x, __fmul_rn(mc.a4, fxx)),
                      __fmaf_rn(mc.a3, inc.y, __fmul_rn(mc.a4, fyy)),
                      __fmaf_rn(mc.a3, inc.z, __fmul_rn(mc.a4, fzz)), 0.f);
@@ -423,19 +442,39 @@ __device__ __forceinline__ void finish_bead(const DevSys& s, int b, int m, float
                                 min_image(__fadd_rn(pi.z, inc.z), boxl), 0.f);
 }
 
+// Completes bead b (of molecule m) from its force sum fs; the step is the
+// molecule's mol_step + STEP + koff, as in k_step, and its parity (which
+// selects the coordinate buffers) is marked in fs.w.
+template <bool STEP>
+__device__ __forceinline__ void finish_bead(const DevSys& s, int b, int m, float4 fs, int koff) {
+  const int cur = (__float_as_int(fs.w) & kOddStep) ? 1 : 0;
+  BeadState t;
+  load_bead_state<STEP>(s, b, m, koff, cur, t);
+  complete_bead<STEP>(s, b, m, fs, cur, t);
+}
+
 // Second kernel of the split step: completes every bead k_step summed
-// (thread per bead, bead order, so every state access is coalesced).
+// (thread per bead, bead order, so every state access is coalesced).  The
+// bead's state and noise do not depend on the force kernel this kernel
+// follows, so they load (and the noise is drawn) before the wait on it:
+// with programmatic dependent launch that work overlaps the force kernel's
+// last blocks.  The force kernel marked the same parity (both read the
+// molecule's step, which only the step advance changes).
 template <bool STEP>
 __global__ void __launch_bounds__(256, 6) k_finish(DevSys s, int koff) {
-  pdl_wait();
-  pdl_release();
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= s.nlive) return;
-  const float4 fs = s.fsum[b];
   const int m = s.mol_of[b];
+  if (m < 0) return;  // a free slot: nothing was summed
+  const int cur = (int)((s.mol_step[m] + (STEP ? 1 : 0) + koff) & 1);
+  BeadState t;
+  load_bead_state<STEP>(s, b, m, koff, cur, t);
+  pdl_wait();
+  pdl_release();
+  const float4 fs = s.fsum[b];
   if (__float_as_int(fs.w) == 0) return;  // not summed this step
   s.fsum[b].w = 0.0f;
-  finish_bead<STEP>(s, b, m, fs, koff);
+  complete_bead<STEP>(s, b, m, fs, cur, t);
 }
 
 // ------------------------------------------------------------ tiled form
