@@ -523,11 +523,11 @@ __global__ void __launch_bounds__(kNlThreads) k_nl(DevSys s) {
   }
 }
 
-// L lanes per bead (8: four beads per warp; 32: a warp per bead, for small
-// contexts, where fewer than a wave of beads leaves the latency of each
-// bead's rounds exposed): the pair list is the in-order compaction of the
-// bead's neighbour-list row by the pair-list cut-off (sop.cu:835-920
-// semantics, host arithmetic of sop.cu:1737-1810).  Each lane takes 4
+// L lanes per bead (8: four beads per warp; 16 for molecules whose rows are
+// long; 32: a warp per bead, for small contexts, where fewer than a wave of
+// beads leaves the latency of each bead's rounds exposed): the pair list is
+// the in-order compaction of the bead's neighbour-list row by the pair-list
+// cut-off (sop.cu:835-920 semantics, host arithmetic of sop.cu:1737-1810).  Each lane takes 4
 // consecutive entries per round (one 8-byte load, four independent gathers)
 // and a scan across the group places the survivors; the attractive pair
 // list is the same over the bead's attractive neighbour list.  The lists do
@@ -693,12 +693,14 @@ void launch_rebin(const DevSys& s, const NLScratch& w, cudaStream_t st) {
 
 void launch_pl_rebuild(const DevSys& s, int koff, cudaStream_t st) {
   const int T = 256;
-  const bool wide = s.nlive <= kWideListBeads;
-  const unsigned grid = cdiv((long long)s.nlive * (wide ? 32 : 8), T);
+  const int L = s.nlive <= kWideListBeads ? 32 : (s.long_rows ? 16 : 8);
+  const unsigned grid = cdiv((long long)s.nlive * L, T);
   if (s.uniform_type)
-    launch_pdl(wide ? k_pl<true, 32> : k_pl<true, 8>, grid, T, st, s, koff);
+    launch_pdl(L == 32 ? k_pl<true, 32> : L == 16 ? k_pl<true, 16> : k_pl<true, 8>, grid, T, st, s,
+               koff);
   else
-    launch_pdl(wide ? k_pl<false, 32> : k_pl<false, 8>, grid, T, st, s, koff);
+    launch_pdl(L == 32 ? k_pl<false, 32> : L == 16 ? k_pl<false, 16> : k_pl<false, 8>, grid, T, st,
+               s, koff);
 }
 
 }  // namespace sop

@@ -71,6 +71,8 @@ struct DevSys {
   float sig2[3][3];             // sigma_rep^2 by type pair
   float rep_tol[3][3];          // sigma_rep * 1e-7: pairs with d^2 <= this are skipped (energy.cu:555-558)
   int uniform_type;             // 1: every bead has type 1 (one sigma for all pairs)
+  int long_rows;                // 1: molecules of 10,000 beads or more (rows of ~400
+                                // neighbours): the pair-list rebuild takes 16 lanes per bead
   unsigned seed_lo, seed_hi;
 
   float4* x[2];
