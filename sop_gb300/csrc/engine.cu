@@ -1759,7 +1759,7 @@ int sop_serve_create(const sop_params* p, long long budget_bytes, long long max_
     return rc;
   }
   ctx->s.uniform_type = 1;
-  ctx->s.long_rows = max_job_beads >= kLongRowBeads ? 1 : 0;
+  ctx->s.long_rows = 0;  // a served mix is mostly molecules far below kLongRowBeads
   ctx->mols.assign(c.mols, HostMol());
   ctx->slot_job.assign(c.mols, -1);
   // a served context fills up and empties as jobs come and go, so its step

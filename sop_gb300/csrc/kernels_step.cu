@@ -466,7 +466,14 @@ __global__ void __launch_bounds__(256, 6) k_finish(DevSys s, int koff) {
   if (b >= s.nlive) return;
   const int m = s.mol_of[b];
   if (m < 0) return;  // a free slot: nothing was summed
-  const int cur = (int)((s.mol_step[m] + (STEP ? 1 : 0) + koff) & 1);
+  // a molecule k_step skips for good (inactive, not started or finished:
+  // the tests of bead_slot on values no kernel of this step writes) has
+  // nothing to finish; a stopped one is caught by its unmarked sum below
+  // (its status bits may be set by this very kernel)
+  const MolConst& mc = s.mol[m];
+  const long long n = s.mol_step[m] + (STEP ? 1 : 0) + koff;
+  if (!mc.active || n < 0 || (STEP && mc.nsteps >= 0 && n > mc.nsteps)) return;
+  const int cur = (int)(n & 1);
   BeadState t;
   load_bead_state<STEP>(s, b, m, koff, cur, t);
   pdl_wait();
@@ -987,12 +994,13 @@ cudaError_t launch_step_persist(const DevSys& s, int G, int koff0, int count, bo
 
 template <int G>
 static cudaError_t launch_block_g(const DevSys& s, int koff0, int count, bool step, cudaStream_t st) {
+  const unsigned B = kBlockFormThreads;
   if (s.uniform_type) {
-    if (step) return launch_pdl(k_step_block<G, true, true>, 1, kBlockFormThreads, st, s, koff0, count);
-    return launch_pdl(k_step_block<G, false, true>, 1, kBlockFormThreads, st, s, koff0, count);
+    if (step) return launch_pdl(k_step_block<G, true, true>, 1, B, st, s, koff0, count);
+    return launch_pdl(k_step_block<G, false, true>, 1, B, st, s, koff0, count);
   }
-  if (step) return launch_pdl(k_step_block<G, true, false>, 1, kBlockFormThreads, st, s, koff0, count);
-  return launch_pdl(k_step_block<G, false, false>, 1, kBlockFormThreads, st, s, koff0, count);
+  if (step) return launch_pdl(k_step_block<G, true, false>, 1, B, st, s, koff0, count);
+  return launch_pdl(k_step_block<G, false, false>, 1, B, st, s, koff0, count);
 }
 
 // Steps koff0 .. koff0 + count - 1 (no list rebuild among them) in one block.

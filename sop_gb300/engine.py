@@ -181,6 +181,26 @@ def baseline_params(**kw) -> Params:
     return default_params(**base)
 
 
+_F32, _I32 = np.dtype(np.float32), np.dtype(np.int32)
+
+
+def _arr(a, dt):
+    """a as a C-contiguous array of dtype dt, without a copy when it is one."""
+    if type(a) is np.ndarray and a.dtype == dt and a.flags.c_contiguous:
+        return a
+    return np.ascontiguousarray(a, dt)
+
+
+def _addr(a):
+    """The address of an array's data as an integer (None for None)."""
+    if a is None:
+        return None
+    try:  # the buffer protocol: about a third of the cost of .ctypes
+        return ctypes.addressof(ctypes.c_char.from_buffer(a))
+    except (TypeError, ValueError, BufferError):  # read-only or empty arrays
+        return a.ctypes.data
+
+
 def _p(a):
     """The address of an array's data (None for None)."""
     if a is None:
@@ -227,18 +247,22 @@ class Engine:
     def add(self, mol: Molecule, xyz: np.ndarray | None = None, T: float = 0.6, traj: int = 0,
             nsteps: int = -1, vel: np.ndarray | None = None, pos: np.ndarray | None = None,
             eps_energy: np.ndarray | None = None) -> int:
-        x = np.ascontiguousarray(mol.xyz if xyz is None else xyz, np.float32)
-        arrs = dict(bi=mol.bond_i, bj=mol.bond_j, br=mol.bond_r0, ai=mol.ang_i, ak=mol.ang_k,
-                    ni=mol.nat_i, nj=mol.nat_j, nr=mol.nat_r0, ne=mol.nat_eps, ty=mol.types)
-        a = {k: np.ascontiguousarray(v, np.float32 if k in ("br", "nr", "ne") else np.int32)
-             for k, v in arrs.items()}
-        v = None if vel is None else np.ascontiguousarray(vel, np.float32)
-        ps = None if pos is None else np.ascontiguousarray(pos, np.float32)
-        ee = None if eps_energy is None else np.ascontiguousarray(eps_energy, np.float32)
-        d = MoleculeDesc(mol.n, len(a["bi"]), _p(a["bi"]), _p(a["bj"]), _p(a["br"]),
-                         len(a["ai"]), _p(a["ai"]), _p(a["ak"]), len(a["ni"]), _p(a["ni"]),
-                         _p(a["nj"]), _p(a["nr"]), _p(a["ne"]), _p(ee), _p(a["ty"]), _p(x),
-                         _p(ps), _p(v), float(T), int(traj), int(nsteps))
+        # arrays already of the right type and layout are passed as they are
+        # (the common case: the generator's), others converted; the
+        # addresses go into the descriptor as plain integers
+        f32, i32 = _F32, _I32
+        x, bi, bj, br = _arr(mol.xyz if xyz is None else xyz, f32), _arr(mol.bond_i, i32), \
+            _arr(mol.bond_j, i32), _arr(mol.bond_r0, f32)
+        ai, ak = _arr(mol.ang_i, i32), _arr(mol.ang_k, i32)
+        ni, nj, nr, ne = _arr(mol.nat_i, i32), _arr(mol.nat_j, i32), _arr(mol.nat_r0, f32), \
+            _arr(mol.nat_eps, f32)
+        ty = _arr(mol.types, i32)
+        v = None if vel is None else _arr(vel, f32)
+        ps = None if pos is None else _arr(pos, f32)
+        ee = None if eps_energy is None else _arr(eps_energy, f32)
+        d = MoleculeDesc(mol.n, len(bi), _addr(bi), _addr(bj), _addr(br), len(ai), _addr(ai),
+                         _addr(ak), len(ni), _addr(ni), _addr(nj), _addr(nr), _addr(ne), _addr(ee),
+                         _addr(ty), _addr(x), _addr(ps), _addr(v), float(T), int(traj), int(nsteps))
         mid = ctypes.c_int()
         self._check(lib().sop_add_molecule(self.h, ctypes.byref(d), ctypes.byref(mid)), self.h)
         self.mols.append(mol)
