@@ -8,18 +8,22 @@ eps = 1, sigma = 3.8, neighbour list 32 A every 50 steps, pair list 16 A every
 10 steps, h = 0.05, zeta = 0.05, started from the native structures.  The step
 loop runs as a CUDA graph of 10 steps per replay; one bench step is one replay
 (10 Langevin steps of every trajectory).  Inputs are the project's seeded
-synthetic structures.
+synthetic structures.  The ensemble is held as two contexts (engine.Ensemble,
+`--parts`), each on its own CUDA stream, cut at equal bead counts: one
+context's list rebuilds and kernel tails overlap the other's step kernels.
 
 Timing: W untimed bench steps, then K bench steps, each bracketed by CUDA
-events on the engine's stream, with a 256 MiB write (flushes the 129 MB L2)
-before every step outside the events; a barrier and synchronize on both sides;
-the max over ranks.  Under torchrun each rank runs its own 512-trajectory
+events (recorded on the first context's stream, which the other streams wait
+on at the start and which waits on them at the end), with a 256 MiB write
+(flushes the 129 MB L2) before every step outside the events; a barrier and
+synchronize on both sides; the max over ranks.  Under torchrun each rank runs its own 512-trajectory
 ensemble (replicas: trajectories are independent, no collective), so the
 scaling is weak.
 
 Beside the headline the line carries:
-  roofline      the step kernel timed alone (algorithmic bytes / CUDA-event
-                time); traffic is a profile figure from the committed ncu capture
+  roofline      the step kernels timed alone, one launch per context on the
+                contexts' streams (algorithmic bytes / CUDA-event time);
+                traffic is a profile figure from the committed ncu capture
   e2e           a 300-step job through the C ABI from host arrays, coordinates
                 copied out every step; set-up time and the steady rate apart
   cpu_baseline  the reference algorithm on all host cores, bounded sample
@@ -90,15 +94,18 @@ def measured_peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def profile_traffic(workload: str = "ensemble") -> float | None:
+def profile_traffic(workload: str = "ensemble", parts: int = 1) -> float | None:
     """DRAM bytes per launch of the step kernel from the committed ncu summary
-    of that workload (None when there is none).  A profile figure: ncu's
-    dram__bytes_read.sum + dram__bytes_write.sum of one capture of the same
-    kernel on the same workload, not measured during this run."""
+    of that workload (None when there is none); with the ensemble split over
+    `parts` contexts, the bytes of one launch of each context's step kernels
+    together.  A profile figure: ncu's dram__bytes_read.sum +
+    dram__bytes_write.sum of one capture of the same kernels on the same
+    workload, not measured during this run."""
     p = os.path.join(ROOT, "profiles", f"step_kernel_{workload}.md")
+    key = "traffic_bytes_per_launch:" if parts <= 1 else f"traffic_bytes_per_launch_{parts}_parts:"
     try:
         for line in open(p):
-            if line.strip().startswith("traffic_bytes_per_launch:"):
+            if line.strip().startswith(key):
                 return float(line.split(":", 1)[1].split()[0])
     except Exception:
         pass
@@ -528,6 +535,9 @@ def main() -> None:
                          "(the steps between rebuilds in one launch); 0: autotuned")
     ap.add_argument("--window", type=int, default=0,
                     help="shared-memory window of the step in beads; 0: autotuned, -1: none")
+    ap.add_argument("--parts", type=int, default=2,
+                    help="ensemble: contexts (each on its own stream) the trajectories are split "
+                         "over, at equal bead counts")
     ap.add_argument("--workload", default="ensemble", choices=["ensemble", *PLAIN],
                     help="ensemble: the batched ensemble (with the served stream beside it); "
                          "plain128 / plain4000 / plain50k: the plain path on one structure")
@@ -566,17 +576,37 @@ def main() -> None:
     total = sum(m.n for m in mols)
     p = engine.baseline_params(device=local, graph_steps=MD_STEPS, lanes_per_bead=args.lanes,
                                step_split=args.form, step_window=args.window)
-    e = engine.Engine(p)
-    for k, (m, t) in enumerate(zip(mols, ts)):
-        e.add(m, m.xyz, T=float(t), traj=rank * N_TRAJ + k)
-    e.commit()
-    stream = torch.cuda.ExternalStream(e.stream(), device=dev)
+
+    def build():
+        # the persistent form (--form 3) runs in one context only
+        ens = engine.Ensemble(p, parts=1 if args.form == 3 else args.parts)
+        for k, (m, t) in enumerate(zip(mols, ts)):
+            ens.add(m, m.xyz, T=float(t), traj=rank * N_TRAJ + k)
+        ens.commit()
+        return ens
+
+    e = build()
+    streams = [torch.cuda.ExternalStream(s, device=dev) for s in e.streams()]
+    s0 = streams[0]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def fork_join(enqueue, ev0, ev1):
+        """ev0 on the first stream, the others wait on it; enqueue(); the
+        first stream waits on the others' ends; ev1 on the first stream."""
+        ev0.record(s0)
+        for st in streams[1:]:
+            st.wait_event(ev0)
+        enqueue()
+        for st in streams[1:]:
+            j = torch.cuda.Event()
+            j.record(st)
+            s0.wait_event(j)
+        ev1.record(s0)
 
     for _ in range(args.warmup):
         e.step_async(MD_STEPS)
     e.sync()
-    s_start = e.status(0)[1]
+    s_start = [eng.status(0)[1] for eng in e.engines]
     tuning = e.tuning()
 
     K = args.steps
@@ -585,40 +615,38 @@ def main() -> None:
     barrier()
     torch.cuda.synchronize(dev)
     with ClockSampler(local) as clk:
-        with torch.cuda.stream(stream):
+        with torch.cuda.stream(s0):
             for k in range(K):
                 flush.zero_()
-                ev[k][0].record(stream)
-                e.step_async(MD_STEPS)
-                ev[k][1].record(stream)
+                fork_join(lambda: e.step_async(MD_STEPS), *ev[k])
         torch.cuda.synchronize(dev)
         e.sync()
     barrier()
     ms = [a.elapsed_time(b) for a, b in ev]
-    s_end = e.status(0)[1]
-    if s_end - s_start != K * MD_STEPS:
+    s_end = [eng.status(0)[1] for eng in e.engines]
+    if any(b - a != K * MD_STEPS for a, b in zip(s_start, s_end)):
         raise RuntimeError("a neighbour-list overflow re-ran steps outside the timed region")
     statuses = [e.status(m)[0] for m in range(len(mols))]
     t_local = sum(ms) / 1e3
     t_max = max_over_ranks(t_local, world, dev)
     value = whole_job_rate(total, MD_STEPS * K, world, t_max)
 
-    # ---- roofline of the dominant kernel (the fused step kernel), timed alone
+    # ---- roofline of the dominant kernel (the fused step kernel), timed alone:
+    # one launch per context, the contexts' launches side by side
     byts, ls = step_kernel_bytes(e, mols)
     reps = 50
     kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(reps)]
-    with torch.cuda.stream(stream):
+    with torch.cuda.stream(s0):
         for k in range(reps):
             flush.zero_()
-            kev[k][0].record(stream)
-            e.launch_stage(0, 0)
-            kev[k][1].record(stream)
+            fork_join(lambda: [eng.launch_stage(0, 0) for eng in e.engines], *kev[k])
     torch.cuda.synchronize(dev)
     t_kernel = statistics.median(a.elapsed_time(b) for a, b in kev) / 1e3
     peak, peak_kind = measured_peaks()
     achieved = byts / t_kernel / 1e9
-    traffic = profile_traffic()
+    traffic = profile_traffic(parts=len(e.engines))
+    n_parts = len(e.engines)
     e.close()
 
     # ---- end to end through the C ABI: host arrays in, coordinates out every step
@@ -632,10 +660,7 @@ def main() -> None:
             h2d += 12 * m.n * 2 + 12 * len(m.bond_i) + 8 * len(m.ang_i) + 16 * len(m.nat_i) + 4 * m.n
         barrier()
         t0 = time.perf_counter()
-        e2 = engine.Engine(p)
-        for k, (m, t) in enumerate(zip(mols, ts)):
-            e2.add(m, m.xyz, T=float(t), traj=rank * N_TRAJ + k)
-        e2.commit()
+        e2 = build()
         t_setup = time.perf_counter() - t0
         # each step's coordinates are copied out while the next step runs:
         # queue step k and its download, then wait for download k-1
@@ -657,11 +682,12 @@ def main() -> None:
                "h2d_bytes_per_step": int(h2d / K2), "d2h_bytes_per_step": int(12 * total),
                "steps": K2, "setup_s": t_setup,
                "steady_value": whole_job_rate(total, MD_STEPS * K2, world, dt - t_setup),
-               "note": f"wall clock of a {K2}-step job through the C ABI: context creation, "
-                       "upload of every structure from host arrays and set-up (setup_s), then "
-                       "per step 10 Langevin steps and a download of every coordinate "
-                       "(sop_download_all_async into page-locked memory, waited for one step "
-                       "later); value includes the set-up, steady_value excludes it"}
+               "note": f"wall clock of a {K2}-step job through the C ABI: creation of the "
+                       f"{n_parts} contexts, upload of every structure from host arrays and "
+                       "set-up (setup_s), then per step 10 Langevin steps and a download of "
+                       "every coordinate (sop_download_all_async of each context into its rows "
+                       "of page-locked memory, waited for one step later); value includes the "
+                       "set-up, steady_value excludes it"}
 
     cpu = None
     plain = None
@@ -698,8 +724,8 @@ def main() -> None:
         served = served_stream(local)
 
     if rank == 0:
-        n_launch = sum(launches_per_bench_step(p, s_start + k * MD_STEPS, tuning.get("form", 1))
-                       for k in range(K))
+        n_launch = sum(launches_per_bench_step(p, s0_ + k * MD_STEPS, tu.get("form", 1))
+                       for s0_, tu in zip(s_start, tuning) for k in range(K))
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / K, "higher_is_better": True,
@@ -710,7 +736,8 @@ def main() -> None:
                          "traffic_source": ("ncu capture of this kernel on this workload, "
                                             "profiles/step_kernel_ensemble.md" if traffic else None),
                          "kernel": "force + Langevin step (k_step; + k_finish in the two-kernel "
-                                   "form)", "step_form": tuning.get("form"),
+                                   "form), one launch per context side by side",
+                         "step_form": [tu.get("form") for tu in tuning],
                          "bytes_per_launch": byts, "launch_us": t_kernel * 1e6,
                          "peak_source": peak_kind},
             "cpu_baseline": cpu,
@@ -723,6 +750,7 @@ def main() -> None:
             "plain": plains,
             "lists": ls,
             "tuning": tuning,
+            "contexts": n_parts,
             "molecule_errors": int(sum(1 for s in statuses if s & 3)),
         }
         print(json.dumps(line), flush=True)

@@ -165,3 +165,40 @@ def test_dropin_program_links_and_reaches_the_engine(tmp_path):
     assert "[Finished reading initial coordinates (32)]" in r.stdout
     if r.returncode != 0:   # no device here: the shim's device query or the engine refuses
         assert "sop_ctx_create failed" in r.stderr or "cudaGetDevice failed" in r.stderr, r.stderr
+
+
+@pytest.mark.parametrize("seed", range(6))
+@pytest.mark.parametrize("parts", [1, 2, 3, 5])
+def test_ensemble_split_by_beads(seed, parts):
+    """The cut of an ensemble into contexts: contiguous, non-empty runs in id
+    order, at most `parts` of them, each within one molecule of an equal
+    share of the beads."""
+    rng = np.random.default_rng(seed)
+    sizes = [int(x) for x in rng.integers(10, 1500, size=int(rng.integers(1, 40)))]
+    cuts = engine.split_by_beads(sizes, parts)
+    assert cuts[0] == 0 and cuts[-1] == len(sizes)
+    assert all(a < b for a, b in zip(cuts, cuts[1:]))
+    assert len(cuts) - 1 == min(parts, len(sizes)) or len(cuts) - 1 < parts
+    total, share = sum(sizes), sum(sizes) / parts
+    acc = np.cumsum([0] + sizes)
+    for k, c in enumerate(cuts[1:-1], start=1):
+        # run k closes at the first molecule reaching k shares
+        assert acc[c] >= k * share and acc[c - 1] < k * share
+    assert engine.split_by_beads([], parts) == [0, 0]
+    assert engine.split_by_beads([10, 10, 10], 10) == [0, 1, 2, 3]
+    assert total == acc[-1]
+
+
+def test_ensemble_refuses_what_it_cannot_run():
+    """parts < 1, the persistent step form beside other contexts, and
+    molecules added after commit (no GPU needed for the checks)."""
+    with pytest.raises(ValueError):
+        engine.Ensemble(engine.default_params(), parts=0)
+    with pytest.raises(ValueError):
+        engine.Ensemble(engine.default_params(step_split=3), parts=2)
+    ens = engine.Ensemble(engine.default_params(step_split=3), parts=1)
+    m = system.generate(60, 0)
+    assert ens.add(m) == 0 and ens.add(m, m.xyz, T=0.7, traj=1) == 1
+    ens.engines = [object()]     # as after commit
+    with pytest.raises(RuntimeError):
+        ens.add(m)

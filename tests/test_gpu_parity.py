@@ -687,3 +687,42 @@ def test_download_all_async_overlaps_and_matches_blocking_downloads():
     assert tickets == [0, 1, 2, 3]
     for g, w in zip(got, want):
         np.testing.assert_array_equal(g, w)
+
+
+def test_ensemble_contexts_bit_identical():
+    """An ensemble split over three contexts on three streams, stepped
+    together across neighbour-list rebuilds, gives the bits of one context
+    holding every molecule: coordinates (blocking and queued downloads in id
+    order), velocities, forces, energies and step counts."""
+    torch = pytest.importorskip("torch")
+    sizes = [(60, 20), (700, 21), (150, 22), (1500, 23), (90, 24), (400, 25), (1200, 26)]
+    mols = [mol_of(n, s) for n, s in sizes]
+    total = sum(m.n for m in mols)
+
+    def make(parts):
+        ens = engine.Ensemble(engine.baseline_params(), parts=parts)
+        for k, m in enumerate(mols):
+            assert ens.add(m, m.xyz, T=0.5 + 0.05 * k, traj=k) == k
+        ens.commit()
+        return ens
+
+    one, three = make(1), make(3)
+    assert len(one.engines) == 1 and len(three.engines) == 3
+    assert three.cuts == engine.split_by_beads([m.n for m in mols], 3)
+    buf = torch.empty((total, 3), dtype=torch.float32, pin_memory=True).numpy()
+    for ens in (one, three):
+        ens.step_async(60)
+        ens.step_async(57)
+    tickets = three.download_all_async(buf)
+    want = one.download_all()
+    three.download_wait(tickets)
+    np.testing.assert_array_equal(buf, want)
+    np.testing.assert_array_equal(three.download_all(), want)
+    for k in range(len(mols)):
+        a, b = one.download(k), three.download(k)
+        for key in ("unc_pos", "vel", "force"):
+            np.testing.assert_array_equal(a[key], b[key])
+        np.testing.assert_array_equal(one.energy(k), three.energy(k))
+        assert one.status(k) == three.status(k) == (0, 117)
+    one.close()
+    three.close()
