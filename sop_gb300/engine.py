@@ -445,6 +445,21 @@ def split_by_beads(sizes, parts: int) -> list[int]:
     return cuts
 
 
+def matched_params(params: Params, tuned: dict) -> Params:
+    """A copy of `params` fixed to the lanes per bead and the step form the
+    tuner chose for a context (Engine.tuning()), without the size-bucket
+    tiles.  Unchanged when it chose the tiles, which the parameters cannot
+    fix, or the one-block form, which the tuner tries only for contexts of up
+    to 2,048 beads.  The window stays as the parameters give it: the tuner uses
+    one only where they fix it."""
+    q = Params.from_buffer_copy(params)
+    if not tuned["buckets"]["tiled"] and tuned["form"] in (1, 2):
+        q.lanes_per_bead = tuned["lanes_per_bead"]
+        q.step_split = tuned["form"]
+        q.step_buckets = -1
+    return q
+
+
 class Ensemble:
     """A batched ensemble held as `parts` contexts (sop_ctx_create each), each
     on its own CUDA stream, stepped together.
@@ -463,6 +478,12 @@ class Ensemble:
     one context holding the whole ensemble.  The persistent step form
     (step_split 3) is refused for parts > 1: its device-wide barrier needs every
     block of its grid resident while another context's kernels run beside it.
+
+    The first context is tuned alone; the others take its lanes per bead and
+    step form (matched_params).  Contexts in different forms gain nothing (the ensemble
+    above, both streams joined every 10 steps: 2.72e9 with one context in the
+    one-kernel form and one in the two-kernel form, 2.95e9 with both in either
+    form, 2.69e9 in one context).
     """
 
     def __init__(self, params: Params | None = None, parts: int = 2):
@@ -490,15 +511,18 @@ class Ensemble:
         if self.engines:
             raise RuntimeError("commit() called twice")
         self.cuts = split_by_beads([m.n for m in self.mols], self.parts)
+        params = self.params
         try:
             for c0, c1 in zip(self.cuts[:-1], self.cuts[1:]):
-                e = Engine(self.params)
+                e = Engine(params)
                 self.engines.append(e)
                 for i in range(c0, c1):
                     mol, xyz, kw = self._pending[i]
                     local = e.add(mol, xyz, **kw)
                     self._where.append((len(self.engines) - 1, local))
                 e.commit()
+                if len(self.engines) == 1:
+                    params = matched_params(self.params, e.tuning())
         except Exception:
             self.close()
             raise

@@ -202,3 +202,20 @@ def test_ensemble_refuses_what_it_cannot_run():
     ens.engines = [object()]     # as after commit
     with pytest.raises(RuntimeError):
         ens.add(m)
+
+
+def test_ensemble_matched_params():
+    """The contexts after the first take its lanes per bead and step form,
+    without the size-bucket tiles; a tiled or one-block choice leaves the
+    parameters as they were; the caller's window and every other field are
+    kept."""
+    p = engine.default_params(step_window=-1, h=0.03)
+    tuned = {"lanes_per_bead": 8, "form": 2, "window": 0, "buckets": {"tiled": False}}
+    q = engine.matched_params(p, tuned)
+    assert (q.lanes_per_bead, q.step_split, q.step_buckets) == (8, 2, -1)
+    assert (q.step_window, q.h, q.nnlup) == (-1, 0.03, p.nnlup)
+    assert (p.lanes_per_bead, p.step_split, p.step_buckets) == (0, 0, 0)   # a copy
+    q = engine.matched_params(p, dict(tuned, buckets={"tiled": True}))
+    assert bytes(q) == bytes(p)
+    q = engine.matched_params(p, dict(tuned, form=4))
+    assert bytes(q) == bytes(p)

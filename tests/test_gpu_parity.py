@@ -693,7 +693,8 @@ def test_ensemble_contexts_bit_identical():
     """An ensemble split over three contexts on three streams, stepped
     together across neighbour-list rebuilds, gives the bits of one context
     holding every molecule: coordinates (blocking and queued downloads in id
-    order), velocities, forces, energies and step counts."""
+    order), velocities, forces, energies and step counts.  The contexts after
+    the first run in its lanes per bead and step form."""
     torch = pytest.importorskip("torch")
     sizes = [(60, 20), (700, 21), (150, 22), (1500, 23), (90, 24), (400, 25), (1200, 26)]
     mols = [mol_of(n, s) for n, s in sizes]
@@ -708,6 +709,10 @@ def test_ensemble_contexts_bit_identical():
 
     one, three = make(1), make(3)
     assert len(one.engines) == 1 and len(three.engines) == 3
+    tuned = three.tuning()
+    if not tuned[0]["buckets"]["tiled"] and tuned[0]["form"] in (1, 2):
+        first = (tuned[0]["lanes_per_bead"], tuned[0]["form"])
+        assert all((t["lanes_per_bead"], t["form"]) == first for t in tuned), tuned
     assert three.cuts == engine.split_by_beads([m.n for m in mols], 3)
     buf = torch.empty((total, 3), dtype=torch.float32, pin_memory=True).numpy()
     for ens in (one, three):
