@@ -94,15 +94,17 @@ def measured_peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def profile_traffic(workload: str = "ensemble", parts: int = 1) -> float | None:
+def profile_traffic(workload: str = "ensemble", parts: int = 0, form: int = 0) -> float | None:
     """DRAM bytes per launch of the step kernel from the committed ncu summary
-    of that workload (None when there is none); with the ensemble split over
-    `parts` contexts, the bytes of one launch of each context's step kernels
-    together.  A profile figure: ncu's dram__bytes_read.sum +
-    dram__bytes_write.sum of one capture of the same kernels on the same
-    workload, not measured during this run."""
+    of that workload (None when there is none).  For the ensemble, `parts`
+    contexts whose step kernels run in `form` (1 one kernel, 2 force + finish):
+    the bytes of one launch of every context's step kernels together.  A
+    profile figure: ncu's dram__bytes_read.sum + dram__bytes_write.sum of one
+    capture of the same kernels on the same workload, not measured during this
+    run."""
     p = os.path.join(ROOT, "profiles", f"step_kernel_{workload}.md")
-    key = "traffic_bytes_per_launch:" if parts <= 1 else f"traffic_bytes_per_launch_{parts}_parts:"
+    key = (f"traffic_bytes_per_launch_{parts}_parts_form{form}:" if parts
+           else "traffic_bytes_per_launch:")
     try:
         for line in open(p):
             if line.strip().startswith(key):
@@ -645,7 +647,8 @@ def main() -> None:
     t_kernel = statistics.median(a.elapsed_time(b) for a, b in kev) / 1e3
     peak, peak_kind = measured_peaks()
     achieved = byts / t_kernel / 1e9
-    traffic = profile_traffic(parts=len(e.engines))
+    forms = {tu.get("form") for tu in tuning}
+    traffic = profile_traffic(parts=len(e.engines), form=forms.pop()) if len(forms) == 1 else None
     n_parts = len(e.engines)
     e.close()
 
