@@ -733,7 +733,9 @@ def main() -> None:
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / K, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_config(total),
+            "config": dict(workload_config(total), contexts=n_parts,
+                           streams=f"{n_parts} contexts, one CUDA stream each, cut at equal "
+                                   "bead counts; joined at every bench step"),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "traffic_source": ("ncu capture of this kernel on this workload, "
