@@ -219,3 +219,60 @@ def test_ensemble_matched_params():
     assert bytes(q) == bytes(p)
     q = engine.matched_params(p, dict(tuned, form=4))
     assert bytes(q) == bytes(p)
+
+
+def test_ensemble_routes_ids_and_rows(monkeypatch):
+    """Host logic of engine.Ensemble with a stand-in context class: molecule
+    ids map to (context, local id) in id order, downloads of every bead land
+    in each context's rows of the caller's array, and the contexts after the
+    first are created with the first one's lanes and form."""
+    made = []
+
+    class FakeEngine:
+        def __init__(self, params):
+            self.params = engine.Params.from_buffer_copy(params)
+            self.mols, self.tags = [], []
+            made.append(self)
+
+        def add(self, mol, xyz=None, **kw):
+            self.mols.append(mol)
+            self.tags.append(kw["traj"])
+            return len(self.mols) - 1
+
+        def commit(self):
+            pass
+
+        def tuning(self):
+            return {"lanes_per_bead": 16, "form": 2, "window": 0, "buckets": {"tiled": False}}
+
+        def status(self, i):
+            return (0, 1000 * len(made) + self.tags[i])
+
+        def download_all(self, out):
+            assert out.flags.c_contiguous and out.shape == (sum(m.n for m in self.mols), 3)
+            out[:] = np.repeat(np.array(self.tags, np.float32), [m.n for m in self.mols])[:, None]
+            return out
+
+        def close(self):
+            pass
+
+    monkeypatch.setattr(engine, "Engine", FakeEngine)
+    sizes = [30, 200, 50, 400, 10, 90, 300]
+    mols = [system.generate(n, k) for k, n in enumerate(sizes)]
+    ens = engine.Ensemble(engine.default_params(), parts=3)
+    for k, m in enumerate(mols):
+        assert ens.add(m, m.xyz, T=0.6, traj=k) == k
+    ens.commit()
+    assert ens.cuts == engine.split_by_beads(sizes, 3) and len(made) == 3
+    assert [t for e in made for t in e.tags] == list(range(len(mols)))
+    assert (made[0].params.lanes_per_bead, made[0].params.step_split) == (0, 0)
+    for e in made[1:]:
+        assert (e.params.lanes_per_bead, e.params.step_split, e.params.step_buckets) == (16, 2, -1)
+    for k in range(len(mols)):
+        ctx = next(c for c in range(3) if ens.cuts[c] <= k < ens.cuts[c + 1])
+        assert ens.status(k) == (0, 1000 * len(made) + k) and ens._where[k][0] == ctx
+    allx = ens.download_all()
+    np.testing.assert_array_equal(allx[:, 0], np.repeat(np.arange(len(mols), dtype=np.float32), sizes))
+    with pytest.raises(RuntimeError):
+        ens.commit()
+    ens.close()
